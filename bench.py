@@ -1,0 +1,295 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the GB300 Toucan netlist simulator.
+
+Workload (default, N=1): the largest synthetic configuration that fits one
+GPU -- a seeded 16M-LUT (3-operand) levelized netlist in 96 levels with 2M
+flip-flops, 8K 64-bit vector ops and 256 memories of 256K x 32 (2R/2W), run
+with 64 independent stimulus streams (1,024 primary-input bits each).  One
+step = every stream advanced by --cycles-per-step cycles.
+
+  value  : stimulus-cycles/s over the timed steps, device time (CUDA events on
+           the library's stream), inputs resident in HBM.
+  e2e    : the same through the C ABI with host buffers: host stimulus table
+           uploaded and result digests read back inside the timed region.
+  --impl reference : the CPU evaluation of the same design on the host cores
+           (the reference has no CPU evaluator of its own: the oracle port is
+           the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "stimulus-cycles/s & LUT-evals/s: batched+learned vs plain, same GB300, bit-exact"
+
+
+def args_parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="largest")
+    p.add_argument("--cycles-per-step", type=int, default=0)
+    p.add_argument("--streams", type=int, default=0)
+    p.add_argument("--groups", type=int, default=4)
+    p.add_argument("--warps", type=int, default=8)
+    p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-cycles", type=int, default=1)
+    p.add_argument("--out", default="")
+    return p.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_design(workload: str, workdir: Path, rank: int):
+    from toucangpurt_gb300 import sim, workloads
+
+    dp, sp = workdir / f"{workload}.bin", workdir / f"{workload}.sym"
+    info = sim.generate(dp, sp, **workloads.design_config(workload))
+    return dp, sp, info
+
+
+def algorithmic_bytes(st: dict, streams: int, cycles: int) -> float:
+    """Algorithmic bytes of `cycles` cycles of `streams` streams: instruction
+    words (4 B per op slot) read once per cycle, plus 0.5 B per state nibble
+    read or written per stream (registers, exchange, memories)."""
+    instr = 4.0 * st["op_slots"]
+    state = 0.5 * (st["l0_reg_reads"] + st["reg_copy_slots"] + st["l0_exg_reads"] + st["exg_copy_slots"]
+                   + st["mem_read_ops"] + st["mem_write_ops"])
+    return cycles * (instr + streams * state)
+
+
+def cpu_baseline(dp, sp, info, workload, streams, cycles, threads):
+    """Oracle port on the host cores, bounded sample of the same workload."""
+    from oracle import pyoracle
+    from toucangpurt_gb300 import sim, workloads
+
+    od = pyoracle.OracleDesign(dp, sp)
+    stim = sim.StimulusSpec(1234, info["pi_ids"], info["pi_bits"], workloads.toggles(workload, info["pi_bits"]))
+    cyc = np.full(streams, cycles, np.uint32)
+    t0 = time.perf_counter()
+    od.run(cyc, stim, threads=threads)
+    dt = time.perf_counter() - t0
+    return streams * cycles / dt, dt
+
+
+def run_reference(a, rank, ws):
+    """Reference arm: CPU evaluation of the workload on all host threads."""
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    from toucangpurt_gb300 import build, workloads
+
+    build.build()
+    pyoracle.build()
+    wd = Path(tempfile.mkdtemp(prefix="tgs_ref_"))
+    dp, sp, info = make_design(a.workload, wd, 0)
+    streams = a.streams or workloads.RUNS[a.workload]["streams"]
+    cyc = a.cpu_sample_cycles
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as po
+    from toucangpurt_gb300 import sim
+
+    od = po.OracleDesign(dp, sp)
+    stim = sim.StimulusSpec(1234, info["pi_ids"], info["pi_bits"], workloads.toggles(a.workload, info["pi_bits"]))
+    c = np.full(streams, cyc, np.uint32)
+    for _ in range(a.warmup):
+        od.run(c, stim, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        od.run(c, stim, threads=threads)
+    dt = time.perf_counter() - t0
+    v = streams * cyc * a.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "stimulus-cycles/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * dt / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8 nibbles", "data": "synthetic (seeded generator)",
+        "config": {"workload": f"{a.workload}: {info['lut_ops']} LUT ops, {streams} streams, {cyc} cycle(s) per step",
+                   "lut_ops": info["lut_ops"]},
+        "lut_evals_per_s": v * info["lut_ops"],
+        "cpu_baseline": {"value": v, "unit": "stimulus-cycles/s", "cores": threads, "kind": "port",
+                         "sample": f"{streams} streams x {cyc} cycle(s) per step, {a.steps} steps"},
+        "e2e": {"value": v, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(a, rank, ws):
+    from toucangpurt_gb300 import build, sim, workloads
+
+    build.build()
+    gpu = int(os.environ.get("LOCAL_RANK", "0"))
+    wd = Path(tempfile.mkdtemp(prefix="tgs_bench_"))
+    dp, sp, info = make_design(a.workload, wd, rank)
+    streams = a.streams or workloads.RUNS[a.workload]["streams"]
+    cps = a.cycles_per_step or (200 if a.workload in ("largest", "learned") else 2000)
+    schedule = 1 if a.schedule == "learned" else 0
+    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule)
+    s.init(gpu, dp, sp, False, False)
+    st = s.design_stats()
+    toggle = workloads.toggles(a.workload, info["pi_bits"])
+    stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], toggle)
+    cyc = np.full(streams, cps, np.uint32)
+    for _ in range(a.warmup):
+        s.batch_run(cyc, stim)
+    barrier(ws)
+    clk = Clocks(gpu)
+    dev_ms = 0.0
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        out = s.batch_run(cyc, stim)
+        dev_ms += out.device_ms
+        launches += out.launches
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    barrier(ws)
+    dev_s = allreduce_max(dev_ms / 1000.0, ws)
+    wall_s = allreduce_max(wall, ws)
+    total_sc = allreduce_sum(float(streams * cps * a.steps), ws)
+    value = total_sc / dev_s
+    e2e = total_sc / wall_s
+    peak, peak_kind = measured_peak()
+    bytes_launch = algorithmic_bytes(st, streams, cps)
+    achieved = bytes_launch / (dev_ms / 1000.0 / a.steps) / 1e9
+    cpu = None
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        cs, cdt = cpu_baseline(dp, sp, info, a.workload, streams, a.cpu_sample_cycles, os.cpu_count() or 1)
+        cpu = {"value": cs, "unit": "stimulus-cycles/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{streams} streams x {a.cpu_sample_cycles} cycle(s) of the same design, {cdt:.1f} s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "stimulus-cycles/s", "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1000 * dev_s / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
+            "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams, {cps} cycles per step",
+                       "streams": streams, "cycles_per_step": cps, "lut_ops": st["lut_ops"],
+                       "partitions": st["partitions"], "schedule": a.schedule, "groups_per_item": st["groups_per_item"],
+                       "threads_per_block": st["threads"], "blocks": st["blocks"],
+                       "l2": "working set (memories) larger than L2"},
+            "lut_evals_per_s": value * st["lut_ops"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind},
+            "e2e": {"value": e2e, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(streams * 8 * 3)},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+        if a.out:
+            Path(a.out).write_text(json.dumps(line) + "\n")
+    s.cleanup()
+
+
+def main():
+    a = args_parse()
+    rank, ws = dist_init()
+    if a.impl == "reference":
+        run_reference(a, rank, ws)
+    else:
+        run_gb300(a, rank, ws)
+
+
+if __name__ == "__main__":
+    main()

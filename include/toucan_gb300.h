@@ -1,0 +1,247 @@
+/* C ABI of the GB300 Toucan netlist simulator.
+ *
+ * Every entry point returns an int status: TGS_OK (0) or a negative TGS_ERR_*
+ * code, with a message retrievable through tgs_last_error() (thread local).
+ * Plain pointers and sizes only; no C++ or CUDA types cross this boundary.
+ *
+ * The reference runtime (ucsc-vama/toucanGPURT) keeps one simulator as
+ * process-global device state (src/SimEval.cu:190-215) behind the C++ class
+ * toucanGPUSim::ToucanSimulator (include/ToucanGPUSim.h:10-74).  Here each
+ * simulator is a handle; the C++ class of the same name (ToucanGPUSim.h in
+ * this directory) wraps one handle.  Each declaration names the reference
+ * function it replaces.
+ *
+ * Value model (shared with the reference): every signal is a 4-bit nibble
+ * stored in one byte; registers and memories are byte arrays (regPool,
+ * memPool) addressed by nibble id.  A "stream" is one independent copy of
+ * the design state driven by its own stimulus; the reference runs exactly
+ * one stream, this library runs many at once.
+ */
+#ifndef TOUCAN_GB300_H
+#define TOUCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TGS_OK = 0,
+  TGS_ERR_ARG = -1,            /* bad argument (null handle, size mismatch...) */
+  TGS_ERR_IO = -2,             /* file cannot be opened / read / written */
+  TGS_ERR_FORMAT = -3,         /* design or symbol stream malformed or truncated */
+  TGS_ERR_INVALID_DESIGN = -4, /* design violates a rule the evaluator relies on */
+  TGS_ERR_CUDA = -5,           /* CUDA runtime error */
+  TGS_ERR_NO_DEVICE = -6,      /* no usable GPU / unsupported compute capability */
+  TGS_ERR_RESOURCES = -7,      /* shared memory, occupancy or co-residency too small */
+  TGS_ERR_TIMEOUT = -8,        /* a device-side barrier wait ran out of its budget */
+  TGS_ERR_STATE = -9,          /* call out of order (e.g. eval before init) */
+  TGS_ERR_NOT_FOUND = -10,     /* unknown register / signal name */
+  TGS_ERR_RANGE = -11,         /* value or size out of range */
+  TGS_ERR_DEVICE_FAULT = -12   /* device-side check failed (address out of range...) */
+};
+
+typedef struct tgs_sim tgs_sim;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *tgs_last_error(void);
+/* Library version string. */
+const char *tgs_version(void);
+
+/* ---- lifetime --------------------------------------------------------- */
+int tgs_create(tgs_sim **out);
+/* Frees all device and host memory of the handle.  The reference's
+ * ToucanSimulator::cleanup (src/ToucanSim.cu:302-304) frees nothing. */
+int tgs_destroy(tgs_sim *h);
+
+/* ---- tuning ----------------------------------------------------------- */
+typedef struct tgs_options {
+  uint32_t n_streams;        /* independent design copies (default 1) */
+  uint32_t warps_per_block;  /* 4, 8, 16 or 32 (0 = autotune / default) */
+  uint32_t groups_per_item;  /* 8-stream groups one block evaluates together: 1, 2, 4 */
+  uint32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid (0 = max) */
+  uint32_t schedule;         /* TGS_SCHED_GREEDY or TGS_SCHED_LEARNED */
+  uint32_t mode;             /* TGS_MODE_PERSISTENT or TGS_MODE_GRAPH */
+  uint32_t barrier_timeout_ms; /* budget of every device-side wait (default 2000) */
+  uint32_t validate;         /* 1 = run the static design checks at init (default 1) */
+  uint32_t resident_netlist; /* 1 = keep each block's netlist in shared memory when it fits */
+  uint32_t reserved[7];
+} tgs_options;
+
+#define TGS_SCHED_GREEDY 0u
+#define TGS_SCHED_LEARNED 1u
+#define TGS_MODE_PERSISTENT 0u
+#define TGS_MODE_GRAPH 1u
+
+int tgs_default_options(tgs_options *opt);
+/* Takes effect at the next tgs_init / tgs_init_from_memory; n_streams and the
+ * schedule may also be changed after init (state is reset to the initial state). */
+int tgs_set_options(tgs_sim *h, const tgs_options *opt);
+int tgs_get_options(const tgs_sim *h, tgs_options *opt);
+
+/* ---- ToucanSimulator API ---------------------------------------------- */
+/* ToucanSimulator::init (src/ToucanSim.cu:102-204): load the design and
+ * symbol files, Init(), optionally Randomize(seed 0), upload.  0 on success,
+ * TGS_ERR_IO where the reference returns -1 for a missing file. */
+int tgs_init(tgs_sim *h, int gpu_id, const char *design_path, const char *symbol_path, int randomize,
+             int enable_print);
+/* Same from in-memory serialized design / symbol streams. */
+int tgs_init_from_memory(tgs_sim *h, int gpu_id, const void *design, size_t design_bytes, const void *symbols,
+                         size_t symbol_bytes, int randomize, int enable_print);
+
+/* ToucanSimulator::eval (src/ToucanSim.cu:206-230): one cycle of every
+ * stream; *stop = sticky stop flag of stream 0 (any stream in batched use). */
+int tgs_eval(tgs_sim *h, int *stop);
+/* ToucanSimulator::eval_free_running (src/ToucanSim.cu:232-267): `cycles`
+ * cycles in one persistent launch; like the reference it does not stop early. */
+int tgs_eval_free_running(tgs_sim *h, uint32_t cycles, int *stop);
+
+/* ToucanSimulator::setRegister / readRegister (src/ToucanSim.cu:271-289,
+ * src/SimEval.cu:1058-1081): value split into nibbles, most significant
+ * first, at most 16 nibbles.  TGS_ERR_RANGE when the value is wider than the
+ * register (the reference asserts).  Stream 0. */
+int tgs_set_register(tgs_sim *h, const char *name, uint64_t value);
+int tgs_read_register(tgs_sim *h, const char *name, uint64_t *value);
+/* Per-stream variants. */
+int tgs_set_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t value);
+int tgs_read_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t *value);
+
+/* ToucanSimulator::readSignal (src/ToucanSim.cu:291-300) is unimplemented in
+ * the reference (returns UINT64_MAX).  Here: TGS_ERR_NOT_FOUND for unknown
+ * names, otherwise *value = UINT64_MAX as in the reference. */
+int tgs_read_signal(tgs_sim *h, const char *name, uint64_t *value);
+
+/* get_real_cycles / setEnablePrint / get_eval_done (src/SimEval.cu:1083-1097) */
+int tgs_get_real_cycles(tgs_sim *h, uint32_t *cycles);
+int tgs_get_cycle_cnt(tgs_sim *h, uint64_t *cycles);
+int tgs_set_enable_print(tgs_sim *h, int enable);
+int tgs_get_eval_done(tgs_sim *h, int *stop);
+
+/* copy_profile_data (src/SimEval.cu:1101-1104): per-partition mean clock64
+ * ticks, "useful" (partition work) and "total" (including barrier wait),
+ * over cycles [PROFILE_START_CYCLE, +PROFILE_COLLECT_CYCLE) of the last
+ * free-running launch.  Here always available (no rebuild needed). */
+int tgs_copy_profile_data(tgs_sim *h, int64_t *useful_ticks, int64_t *total_ticks, size_t count);
+
+/* ---- bulk state access (new) ------------------------------------------ */
+int tgs_get_pool_sizes(const tgs_sim *h, uint32_t *reg_pool, uint32_t *mem_pool, uint32_t *exchange_pool);
+/* Full regPool / memPool of one stream (reference byte layout). */
+int tgs_read_reg_pool(tgs_sim *h, uint32_t stream, uint8_t *out, size_t bytes);
+int tgs_write_reg_pool(tgs_sim *h, uint32_t stream, const uint8_t *in, size_t bytes);
+int tgs_read_mem_pool(tgs_sim *h, uint32_t stream, uint8_t *out, size_t bytes);
+int tgs_write_mem_pool(tgs_sim *h, uint32_t stream, const uint8_t *in, size_t bytes);
+/* Digests as defined for the oracle: sum over i of mix64((i << 8) | pool[i]). */
+int tgs_state_digest(tgs_sim *h, uint32_t stream, uint64_t *reg_digest, uint64_t *mem_digest);
+/* Reset every stream to the initial state (Init/Randomize result). */
+int tgs_reset_state(tgs_sim *h);
+
+/* ---- batched stimulus runs (new) -------------------------------------- */
+/* Stimulus: the listed register nibbles are rewritten before every cycle.
+ *   seed_s = mix64(base_seed ^ s); h = mix64(seed_s ^ mix64((c << 32) | i))
+ *   toggle[i] == 0: value = h & mask(bits[i]); else the value flips (xor
+ *   mask) when (h >> 48) < toggle[i].  mix64 = splitmix64 finaliser. */
+typedef struct tgs_stimulus {
+  uint64_t base_seed;
+  uint32_t n_inputs;
+  const uint32_t *reg;     /* regPool nibble ids */
+  const uint8_t *bits;     /* bit width of each input nibble (1..4) */
+  const uint16_t *toggle;  /* NULL = all inputs uniform */
+} tgs_stimulus;
+
+#define TGS_BATCH_CYCLE_DIGESTS 1u /* fill cycle_digest[] */
+#define TGS_BATCH_ROLLING 2u       /* fill rolling_digest[] */
+#define TGS_BATCH_FINAL_STATE 4u   /* fill final_regs[] / final_mems[] */
+
+typedef struct tgs_batch {
+  uint32_t n_streams;       /* streams in the job (may exceed resident slots) */
+  const uint32_t *cycles;   /* cycles per stream */
+  const tgs_stimulus *stim; /* NULL = free running */
+  uint32_t flags;
+  uint32_t slots;           /* resident streams (multiple of 8, 0 = options.n_streams) */
+} tgs_batch;
+
+typedef struct tgs_batch_result {
+  uint64_t *final_reg_digest; /* [n_streams] */
+  uint64_t *final_mem_digest; /* [n_streams] */
+  uint64_t *rolling_digest;   /* [n_streams]: roll = mix64(roll + digest(c)) */
+  uint64_t *cycle_digest;     /* [n_streams * cycle_stride] */
+  uint32_t cycle_stride;
+  uint32_t *stop_cycle;       /* [n_streams], 0xFFFFFFFF = no stop */
+  uint8_t *final_regs;        /* [n_streams * regPoolSize] */
+  uint8_t *final_mems;        /* [n_streams * memPoolSize] */
+  double device_ms;           /* time of the device work */
+  uint64_t stream_cycles;     /* total simulated stream-cycles */
+  uint32_t launches;          /* kernel launches issued */
+} tgs_batch_result;
+
+/* Runs every stream of the job from the initial state.  Streams beyond the
+ * resident slots are queued; a slot whose stream finished is refilled in
+ * place by the next queued stream. */
+int tgs_batch_run(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res);
+
+/* ---- design statistics and launch shape (new) ------------------------- */
+typedef struct tgs_design_stats {
+  uint64_t lut_ops;          /* table lookups (lutIndex != 0) */
+  uint64_t nop_ops;          /* moves (lutIndex == 0) */
+  uint64_t writeback_ops;    /* micro-partition write-back lanes */
+  uint64_t l0_reg_reads, l0_exg_reads;
+  uint64_t reg_copy_slots, exg_copy_slots; /* nibbles moved by the block copies */
+  uint64_t mem_read_ops, mem_write_ops, vec_ops, vec_read_ops, print_ops, stop_ops;
+  uint64_t op_slots;         /* every op slot, 32-bit words of instruction per cycle */
+  uint32_t partitions, mparts, max_value_pool, max_exec_levels;
+  uint32_t blocks, threads, groups_per_item, streams_per_word;
+  uint64_t block_barriers, exec_levels;   /* block barriers kept / exec levels, all partitions */
+  double makespan[2];        /* scheduled cost of the slowest block per region */
+  uint32_t reserved[8];
+} tgs_design_stats;
+int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *out);
+
+/* ---- synthetic designs (new; the reference ships no design or compiler) */
+typedef struct tgs_gen_config {
+  uint64_t seed;
+  uint64_t n_lut;          /* LUT ops with a table lookup */
+  uint32_t levels;         /* logic levels per cycle (split over the two regions) */
+  uint32_t operands;       /* 2 (op0 = 0) or 3 nibble operands per LUT */
+  uint32_t ff_bits;        /* flip-flop bits (4 per register nibble) */
+  uint32_t pi_bits;        /* primary-input bits (register nibbles rewritten by the stimulus) */
+  uint32_t reset_inputs;   /* extra 1-bit primary inputs */
+  uint32_t n_mems, mem_depth, mem_width, mem_read_ports, mem_write_ports;
+  uint32_t mem_multi_writer; /* 1: index = memBase + (addr << 2) */
+  uint32_t n_vec_ops, vec_nibbles;
+  uint32_t palette_pct;    /* % of LUTs using AND/OR/XOR/MUX windows */
+  float fanout_alpha;      /* power-law exponent of operand popularity (0 = uniform) */
+  uint32_t max_fanout;
+  uint32_t luts_per_part;  /* partition size target */
+  uint32_t mpart_width;    /* lanes per micro-partition level (<= 32) */
+  uint32_t cone_depth;     /* logic levels per micro-partition (1 = top level only) */
+  uint32_t mixed;          /* 1: heterogeneous regions (datapath / control / memory / fan-out) */
+  uint32_t with_stop;      /* add a stop op (and print) that fires when a counter saturates */
+  uint32_t reserved[6];
+} tgs_gen_config;
+
+typedef struct tgs_gen_info {
+  uint64_t lut_ops, nop_ops, mparts, partitions;
+  uint64_t mem_read_ops, mem_write_ops, vec_ops, l0_ops;
+  uint32_t reg_pool, mem_pool, exchange_pool, max_value_pool;
+  uint32_t n_pi_nibbles;   /* primary-input nibble ids are listed by tgs_gen_inputs */
+  uint32_t reserved[7];
+} tgs_gen_info;
+
+int tgs_default_gen_config(tgs_gen_config *cfg);
+/* Generates a design, writes the design and symbol files (reference format). */
+int tgs_generate(const tgs_gen_config *cfg, const char *design_path, const char *symbol_path, tgs_gen_info *info);
+/* Primary-input nibble ids and widths of a design generated with cfg
+ * (ids: [n], bits: [n]; n from tgs_gen_info.n_pi_nibbles). */
+int tgs_gen_inputs(const tgs_gen_config *cfg, uint32_t *ids, uint8_t *bits, uint32_t n);
+
+/* Static checks of a design file: the rules that make a design's values
+ * independent of the schedule (def-before-use, no same-level slot conflicts,
+ * word-aligned block copies, table bounds, nibble-valued tables). */
+int tgs_validate_file(const char *design_path, const char *symbol_path, uint64_t *lut_ops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,763 @@
+// GB300 (sm_103a) cycle kernel of the Toucan netlist evaluation.
+//
+// Restates the reference device code (src/SimEval.cu:304-1056) for many
+// stimulus streams at once:
+//   * one 32-bit word per value-pool slot carries the nibbles of 8 streams
+//     (SPW = 8; SPW = 1 runs a single stream in nibble 0), so every
+//     __shfl_sync of a micro-partition level moves 8 streams' operands and
+//     the 4,642-entry truth table is indexed once per stream from shared
+//     memory, where a cp.async.bulk copy staged it at kernel start (the
+//     reference reads __constant__ memory with lane-divergent addresses,
+//     SimEval.cu:190,354,411);
+//   * a block evaluates G 8-stream groups of a partition together, giving G
+//     independent dependency chains per warp level (G words per slot in
+//     shared memory, read with one vector load);
+//   * one persistent cooperative launch runs many cycles; regions are
+//     separated by a software grid barrier whose waits are bounded by a
+//     global-timer budget (timeouts set an error word instead of hanging);
+//   * partitions are statically assigned to blocks and micro-partitions to
+//     warps by the host schedule (greedy gate count or learned cost).
+// All mutable device state (registers, exchange, memories) is read with
+// L1-bypassing loads because other blocks write it between barriers.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "devimage.h"
+#include "kernels.h"
+
+namespace tgs {
+namespace {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t rep8(uint32_t v) { return v * 0x11111111u; }
+__device__ __forceinline__ uint32_t nib(uint32_t w, uint32_t k) { return (w >> (4u * k)) & 0xFu; }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned long long dmix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ void raiseErr(const KParams &p, uint32_t code, uint32_t a, uint32_t b, uint32_t c) {
+  if (atomicCAS(p.err, 0u, code) == 0u) {
+    p.errInfo[0] = code;
+    p.errInfo[1] = a;
+    p.errInfo[2] = b;
+    p.errInfo[3] = c;
+  }
+}
+
+// ---- truth-table lookup ---------------------------------------------------
+// index = lutIndex + (a << 8 | b << 4 | c) per stream (SimEval.cu:353,410).
+template <int SPW>
+__device__ __forceinline__ uint32_t lookup(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
+                                           uint32_t C);
+
+template <>
+__device__ __forceinline__ uint32_t lookup<1>(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
+                                              uint32_t C) {
+  return tab[base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u))];
+}
+
+// 8 streams: even streams sit in the low nibble of each byte, odd streams in
+// the high nibble.  (b << 4 | c) of 4 streams is formed per byte lane with
+// masks, the a nibble is paired with it by byte permutes into two 12-bit
+// indices per word, and the 8 table bytes are packed back with shifts.
+template <>
+__device__ __forceinline__ uint32_t lookup<8>(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
+                                              uint32_t C) {
+  const uint8_t *t = tab + base;
+  const uint32_t bcE = ((B & 0x0F0F0F0Fu) << 4) | (C & 0x0F0F0F0Fu);
+  const uint32_t bcO = (B & 0xF0F0F0F0u) | ((C >> 4) & 0x0F0F0F0Fu);
+  const uint32_t aE = A & 0x0F0F0F0Fu, aO = (A >> 4) & 0x0F0F0F0Fu;
+  const uint32_t e01 = __byte_perm(bcE, aE, 0x5140), e23 = __byte_perm(bcE, aE, 0x7362);
+  const uint32_t o01 = __byte_perm(bcO, aO, 0x5140), o23 = __byte_perm(bcO, aO, 0x7362);
+  const uint32_t r0 = t[e01 & 0xFFFFu], r2 = t[e01 >> 16], r4 = t[e23 & 0xFFFFu], r6 = t[e23 >> 16];
+  const uint32_t r1 = t[o01 & 0xFFFFu], r3 = t[o01 >> 16], r5 = t[o23 & 0xFFFFu], r7 = t[o23 >> 16];
+  const uint32_t lo = r0 | (r2 << 8) | (r4 << 16) | (r6 << 24);
+  const uint32_t hi = r1 | (r3 << 8) | (r5 << 16) | (r7 << 24);
+  return lo | (hi << 4);
+}
+
+// ---- value-pool words of G groups ----------------------------------------
+template <int G>
+__device__ __forceinline__ void loadG(const uint32_t *__restrict__ src, uint32_t (&v)[G]) {
+  if constexpr (G == 4) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(src);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else if constexpr (G == 2) {
+    const uint2 q = *reinterpret_cast<const uint2 *>(src);
+    v[0] = q.x; v[1] = q.y;
+  } else {
+    v[0] = *src;
+  }
+}
+
+// global (mutable state, L1 bypass) -> shared
+template <int G>
+__device__ __forceinline__ void copyInG(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src) {
+  if constexpr (G == 4) {
+    *reinterpret_cast<uint4 *>(dst) = __ldcg(reinterpret_cast<const uint4 *>(src));
+  } else if constexpr (G == 2) {
+    *reinterpret_cast<uint2 *>(dst) = __ldcg(reinterpret_cast<const uint2 *>(src));
+  } else {
+    *dst = __ldcg(src);
+  }
+}
+
+template <int G>
+__device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src) {
+  if constexpr (G == 4) {
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(src);
+  } else if constexpr (G == 2) {
+    *reinterpret_cast<uint2 *>(dst) = *reinterpret_cast<const uint2 *>(src);
+  } else {
+    *dst = *src;
+  }
+}
+
+// ---- micro-partitions (evalSingleMicroPart, SimEval.cu:304-580) -----------
+template <int SPW, int G>
+__device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_t hdr, uint32_t *__restrict__ vp,
+                                        const uint8_t *__restrict__ tab, uint32_t lane) {
+  const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
+  const uint32_t *top = mp + kMPHeaderWords;
+  uint32_t v[G];
+  // top level: operands < 16 are immediates, else value-pool slots
+  if (lane < W) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2 *>(top) + lane);
+    const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
+    uint32_t A[G], B[G], C[G];
+    if (a < 16) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) A[g] = rep8(a);
+    } else {
+      loadG<G>(vp + a * G, A);
+    }
+    if (b < 16) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) B[g] = rep8(b);
+    } else {
+      loadG<G>(vp + b * G, B);
+    }
+    if (c < 16) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) C[g] = rep8(c);
+    } else {
+      loadG<G>(vp + c * G, C);
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
+  } else {
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = 0;
+  }
+  // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
+  const uint32_t *mid = top + 2 * W;
+  for (uint32_t m = 0; m < nMid; ++m) {
+    const uint32_t w = lane < W ? __ldg(mid + m * W + lane) : 0u;
+    const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
+    uint32_t nv[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const uint32_t As = __shfl_sync(kFull, v[g], int(a6 & 31u));
+      const uint32_t Bs = __shfl_sync(kFull, v[g], int(b6 & 31u));
+      const uint32_t Cs = __shfl_sync(kFull, v[g], int(c6 & 31u));
+      const uint32_t A = a6 < 32 ? rep8(a6) : As;
+      const uint32_t B = b6 < 32 ? rep8(b6) : Bs;
+      const uint32_t C = c6 < 32 ? rep8(c6) : Cs;
+      nv[g] = lut ? lookup<SPW>(tab, lut, A, B, C) : C;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) v[g] = nv[g];
+  }
+  // write-back: shuffleId < 32 immediate, else lane (shuffleId mod 32)
+  const uint32_t *wb = mid + nMid * W;
+  const uint32_t wv = lane < nWB ? __ldg(wb + lane) : 0u;
+  const uint32_t src = wv & 0xFFu, res = wv >> 16;
+  uint32_t out[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const uint32_t x = __shfl_sync(kFull, v[g], int(src & 31u));
+    out[g] = src < 32 ? rep8(src) : x;
+  }
+  if (lane < nWB) {
+#pragma unroll
+    for (int g = 0; g < G; ++g) vp[res * G + g] = out[g];
+  }
+}
+
+template <int SPW, int G>
+__device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp,
+                                            uint32_t hdr, uint32_t *__restrict__ vp, uint32_t lane) {
+  const uint32_t n = (hdr >> 2) & 63u;
+  if (lane >= n) return;
+  const uint32_t *r = mp + kMPHeaderWords + lane * kVecReadWords;
+  const uint32_t w0 = __ldg(r), w1 = __ldg(r + 1), w2 = __ldg(r + 2), w3 = __ldg(r + 3), w4 = __ldg(r + 4);
+  const uint32_t base = w0 & 0xFFFFu, len = w0 >> 16, off = w1 & 0xFFFFu, isConst = (w1 >> 16) & 1u;
+  const uint32_t ix[4] = {w2 & 0xFFFFu, w2 >> 16, w3 & 0xFFFFu, w3 >> 16};
+  const uint32_t outR = w4 & 0xFFFFu, res = w4 >> 16;
+  const uint8_t *cv = p.constVec + d.constOff;
+#pragma unroll 1
+  for (int g = 0; g < G; ++g) {
+    uint32_t I[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : vp[ix[j] * G + g];
+    const uint32_t OR = outR < 16 ? rep8(outR) : vp[outR * G + g];
+    uint32_t out = 0;
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) {
+      const uint32_t o = ((nib(I[0], k) << 12) | (nib(I[1], k) << 8) | (nib(I[2], k) << 4) | nib(I[3], k)) + off;
+      uint32_t val;
+      if (o < len)
+        val = isConst ? uint32_t(cv[base + o]) & 15u : nib(vp[(base + o) * G + g], k);
+      else
+        val = nib(OR, k);
+      out |= val << (4 * k);
+    }
+    vp[res * G + g] = out;
+  }
+}
+
+// Signed vector arithmetic on up to 31 nibbles per stream (SimEval.cu:482-548):
+// nibble i of the vector sits in slot base + i, sign bit at 4 * len - 1.
+template <int SPW, int G>
+__device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp, uint32_t hdr,
+                          uint32_t *__restrict__ vp, uint32_t lane) {
+  const uint32_t n = (hdr >> 2) & 63u;
+  if (lane >= n) return;
+  const uint32_t *r = mp + kMPHeaderWords + lane * kVecOpWords;
+  const uint32_t w0 = __ldg(r), w1 = __ldg(r + 1), res = __ldg(r + 2);
+  const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = w1 & 0xFFFFu, op = (w1 >> 16) & 0xFFu, cf = w1 >> 24;
+  const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
+  const uint8_t *cv = p.constVec + d.constOff;
+  const bool isVec = op <= 2;
+  const uint32_t sign = 4 * len - 1;
+#pragma unroll 1
+  for (int g = 0; g < G; ++g) {
+#pragma unroll 1
+    for (int k = 0; k < SPW; ++k) {
+      unsigned __int128 a = 0, b = 0;
+      for (uint32_t i = 0; i < len; ++i) {
+        const uint32_t x = c1 ? (uint32_t(cv[v1 + i]) & 15u) : nib(vp[(v1 + i) * G + g], k);
+        const uint32_t y = c2 ? (uint32_t(cv[v2 + i]) & 15u) : nib(vp[(v2 + i) * G + g], k);
+        a |= (unsigned __int128)x << (4 * i);
+        b |= (unsigned __int128)y << (4 * i);
+      }
+      if ((a >> sign) & 1) a |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
+      if ((b >> sign) & 1) b |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
+      const __int128 sa = (__int128)a, sb = (__int128)b;
+      unsigned __int128 rv = 0;
+      uint32_t bit = 0;
+      switch (op) {
+        case 0: rv = a + b; break;
+        case 1: rv = a - b; break;
+        case 2: rv = a * b; break;
+        case 3: bit = sa == sb; break;
+        case 4: bit = sa < sb; break;
+        case 5: bit = sa <= sb; break;
+        default: bit = 0; break;
+      }
+      const uint32_t kmask = ~(15u << (4 * k));
+      if (isVec) {
+        for (uint32_t i = 0; i < len; ++i) {
+          const uint32_t s = (res + i) & 0xFFFFu;
+          const uint32_t nv = uint32_t(rv >> (4 * i)) & 15u;
+          vp[s * G + g] = (k == 0 ? 0u : (vp[s * G + g] & kmask)) | (nv << (4 * k));
+        }
+      } else {
+        vp[res * G + g] = (k == 0 ? 0u : (vp[res * G + g] & kmask)) | (bit << (4 * k));
+      }
+    }
+  }
+}
+
+template <int SPW, int G>
+__device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__restrict__ mp, uint32_t hdr,
+                                            uint32_t *__restrict__ vp, uint32_t lane, uint32_t gb) {
+  const uint32_t n = (hdr >> 2) & 63u;
+  if (lane >= n) return;
+  const uint32_t *r = mp + kMPHeaderWords + lane * kMemReadWords;
+  const uint32_t lo = __ldg(r), hi = __ldg(r + 1), w2 = __ldg(r + 2), res = __ldg(r + 3);
+  const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
+  const bool multi = (hi >> 31) != 0;
+  const uint32_t en = w2 & 0xFFFFu, av = w2 >> 16;
+#pragma unroll 1
+  for (int g = 0; g < G; ++g) {
+    const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+    uint32_t AD[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) AD[j] = vp[(av + j) * G + g];
+    uint32_t out = vp[res * G + g];  // a disabled read leaves the slot as it is
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) {
+      const uint32_t s = (gb * G + g) * SPW + k;
+      if (s >= p.nStreams || nib(EN, k) == 0) continue;
+      uint32_t addr = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) addr |= nib(AD[j], k) << (4 * j);
+      if (multi) addr <<= 2;
+      const unsigned long long idx = memBase + addr;
+      if (idx >= p.memPoolSize) {
+        raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
+        continue;
+      }
+      const uint32_t val = __ldcg(p.mems + s * p.memStride + idx) & 15u;
+      out = (out & ~(15u << (4 * k))) | (val << (4 * k));
+    }
+    vp[res * G + g] = out;
+  }
+}
+
+// ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
+template <int SPW, int G>
+__device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__ vp, const uint8_t *__restrict__ tab,
+                         uint32_t cycle) {
+  const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
+  const PartDesc &d = p.parts[pid];
+  const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
+
+  // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
+  {
+    const uint32_t n = d.l0Count;
+    const uint32_t *src = p.net + d.l0Off;
+    const uint32_t *dst = src + n;
+    const uint32_t *pool = d.l0Exchange ? p.exg : p.regs;
+    for (uint32_t i = tid; i < n; i += nthr) {
+      const uint32_t s = __ldg(src + i);
+      const uint32_t r = (__ldg(dst + (i >> 1)) >> ((i & 1u) * 16)) & 0xFFFFu;
+      copyInG<G>(vp + r * G, pool + size_t(s) * p.gpad + gb * G);
+    }
+  }
+  __syncthreads();
+
+  // exec levels: warp w runs the micro-partitions the schedule gave it
+  const uint32_t *sc = p.sched + d.schedOff;
+  for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
+    const uint32_t flags = __ldg(sc);
+    if (lv > 0 && (flags & 1u)) __syncthreads();
+    const uint32_t ub = __ldg(sc + 1 + warp), ue = __ldg(sc + 2 + warp);
+    const uint32_t *units = sc + 2 + NW;
+    for (uint32_t u = ub; u < ue; ++u) {
+      const uint32_t *mp = p.net + __ldg(units + u);
+      const uint32_t hdr = __ldg(mp);
+      switch (hdr & 3u) {
+        case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;
+        case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane); break;
+        case kMPVecOp: evalVecOp<SPW, G>(p, d, mp, hdr, vp, lane); break;
+        default: evalMemRead<SPW, G>(p, mp, hdr, vp, lane, gb); break;
+      }
+      __syncwarp();
+    }
+    sc = units + __ldg(sc + 1 + NW);
+  }
+  __syncthreads();
+
+  // last level (evalLastLevel / evalLastLevelExgWrite, SimEval.cu:625-761)
+  if (d.copyKind) {
+    uint32_t *pool = d.copyKind == 1 ? p.regs : p.exg;
+    for (uint32_t i = tid; i < d.copySlots; i += nthr)
+      copyOutG<G>(pool + size_t(d.copyDst + i) * p.gpad + gb * G, vp + (d.copySrc + i) * G);
+  }
+  if (d.copyKind != 2) {
+    for (uint32_t i = tid; i < d.memWCount * G; i += nthr) {
+      const uint32_t opi = i / G, g = i % G;
+      const uint32_t *r = p.net + d.memWOff + 4 * opi;
+      const uint32_t lo = __ldg(r), hi = __ldg(r + 1), w2 = __ldg(r + 2), en = __ldg(r + 3);
+      const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
+      const bool multi = (hi >> 31) != 0;
+      const uint32_t av = w2 & 0xFFFFu, dat = w2 >> 16;
+      const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+      const uint32_t DAT = dat < 16 ? rep8(dat) : vp[dat * G + g];
+      uint32_t AD[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) AD[j] = vp[(av + j) * G + g];
+#pragma unroll
+      for (int k = 0; k < SPW; ++k) {
+        const uint32_t s = (gb * G + g) * SPW + k;
+        if (s >= p.nStreams || nib(EN, k) == 0) continue;
+        uint32_t addr = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) addr |= nib(AD[j], k) << (4 * j);
+        if (multi) addr <<= 2;
+        const unsigned long long idx = memBase + addr;
+        if (idx >= p.memPoolSize) {
+          raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
+          continue;
+        }
+        p.mems[s * p.memStride + idx] = uint8_t(nib(DAT, k));
+      }
+    }
+    if (p.enablePrint) {
+      for (uint32_t i = tid; i < d.printCount * G; i += nthr) {
+        const uint32_t w = __ldg(p.net + d.printOff + i / G), g = i % G;
+        const uint32_t en = w & 0xFFFFu, msg = w >> 16;
+        const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+        for (int k = 0; k < SPW; ++k) {
+          const uint32_t s = (gb * G + g) * SPW + k;
+          if (s < p.nStreams && nib(EN, k) != 0 && msg < p.nPrintMsgs) printf("%s", p.printMsgs[msg]);
+        }
+      }
+    }
+    for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
+      const uint32_t opi = i / G, g = i % G;
+      const uint32_t en = __ldg(p.net + d.stopOff + opi);
+      const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+      for (int k = 0; k < SPW; ++k) {
+        const uint32_t s = (gb * G + g) * SPW + k;
+        if (s >= p.nStreams || nib(EN, k) == 0) continue;
+        if (atomicExch(p.stop + s, 1u) == 0u) {
+          p.stopCycle[s] = cycle;
+          if (p.printDiag) {
+            printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, en, nib(EN, k));
+            for (uint32_t q = 0; q < d.printCount; ++q) {
+              const uint32_t w = __ldg(p.net + d.printOff + q);
+              if ((w & 0xFFFFu) == en && (w >> 16) < p.nPrintMsgs)
+                printf("Stop-associated message (literal): %s\n", p.printMsgs[w >> 16]);
+            }
+          }
+        }
+      }
+    }
+  }
+  // the next item reuses the value pool
+  __syncthreads();
+}
+
+// ---- stimulus / digests ------------------------------------------------------
+template <int SPW>
+__device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
+  const uint32_t total = p.nStim * p.gpad;
+  for (uint32_t i = gtid; i < total; i += gthreads) {
+    const uint32_t inp = i / p.gpad, g = i % p.gpad;
+    const uint32_t reg = __ldg(p.stimReg + inp);
+    const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
+    const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
+    uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
+    const uint32_t w = __ldcg(wp);
+    uint32_t nw = 0;
+    const unsigned long long key = dmix64((unsigned long long)cycle << 32 | inp);
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) {
+      const uint32_t s = g * SPW + k;
+      const uint32_t cur = nib(w, k);
+      uint32_t v = cur;
+      if (s < p.nStreams) {
+        const unsigned long long h = dmix64(__ldg(p.streamSeed + s) ^ key);
+        if (tog == 0)
+          v = uint32_t(h) & mask;
+        else if ((h >> 48) < tog)
+          v = cur ^ mask;
+      }
+      nw |= v << (4 * k);
+    }
+    *wp = nw;
+  }
+}
+
+// Per-cycle register digest: sum over i of mix64(i << 8 | nibble), per stream.
+template <int SPW>
+__device__ void digestSlice(const KParams &p) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  const uint32_t chunks = (p.regSlots + 255) / 256;
+  const uint32_t units = chunks * p.gpad;
+  for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
+    const uint32_t g = u % p.gpad, ch = u / p.gpad;
+    unsigned long long acc[SPW];
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) acc[k] = 0;
+    const uint32_t end = min(p.regSlots, ch * 256 + 256);
+    for (uint32_t i = ch * 256 + lane; i < end; i += 32) {
+      const uint32_t w = __ldcg(p.regs + size_t(i) * p.gpad + g);
+#pragma unroll
+      for (int k = 0; k < SPW; ++k) acc[k] += dmix64((unsigned long long)i << 8 | nib(w, k));
+    }
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) {
+      unsigned long long a = acc[k];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+      const uint32_t s = g * SPW + k;
+      if (lane == 0 && s < p.nStreams) atomicAdd(p.digAcc + s, a);
+    }
+  }
+}
+
+__device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
+  for (uint32_t s = gtid; s < p.nStreams; s += gthreads) {
+    const unsigned long long dg = __ldcg(p.digAcc + s);
+    p.digAcc[s] = 0;
+    p.roll[s] = dmix64(p.roll[s] + dg);
+    if (p.cycDig && cycle < p.cycStride) p.cycDig[size_t(s) * p.cycStride + cycle] = dg;
+  }
+}
+
+// ---- grid barrier (bounded) --------------------------------------------------
+__device__ __forceinline__ bool gridSync(const KParams &p, uint32_t &gen) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const uint32_t target = gen + 1;
+    __threadfence();
+    const uint32_t arrived = atomicAdd(p.barrier, 1u);
+    if (arrived == p.nBlocks - 1) {
+      atomicExch(p.barrier, 0u);
+      __threadfence();
+      atomicExch(p.barrier + 1, target);
+    } else {
+      const unsigned long long t0 = gtimer();
+      volatile uint32_t *vg = p.barrier + 1;
+      volatile uint32_t *ve = p.err;
+      while (int32_t(*vg - target) < 0) {
+        if (*ve != 0u) { ok = 0; break; }
+        if (gtimer() - t0 > p.timeoutNs) {
+          raiseErr(p, kErrTimeout, blockIdx.x, target, 0);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    gen = target;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Stages the truth table into shared memory with one bulk async copy.
+__device__ bool stageTable(const KParams &p, uint8_t *tab) {
+  __shared__ __align__(8) unsigned long long mbar;
+  const uint32_t mb = uint32_t(__cvta_generic_to_shared(&mbar));
+  const uint32_t dst = uint32_t(__cvta_generic_to_shared(tab));
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(kLutTablePadded) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(p.lutTable), "r"(kLutTablePadded), "r"(mb)
+                 : "memory");
+  }
+  uint32_t done = 0;
+  const unsigned long long t0 = gtimer();
+  while (!done) {
+    asm volatile(
+        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], 0;\n\tselp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(done)
+        : "r"(mb)
+        : "memory");
+    if (!done && gtimer() - t0 > p.timeoutNs) {
+      raiseErr(p, kErrTimeout, blockIdx.x, 0xFFFFFFFFu, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+// ---- kernels -----------------------------------------------------------------
+template <int SPW, int G>
+__global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0, uint32_t nCycles) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint8_t *tab = smem;
+  uint32_t *vp = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
+  const bool staged = stageTable(p, tab);
+  __syncthreads();
+  if (!staged) return;
+  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
+  uint32_t gen = 0;
+  if (p.flags & kFlagStimulus) {
+    applyStimulus<SPW>(p, c0, gtid, gthreads);
+    if (!gridSync(p, gen)) return;
+  }
+  for (uint32_t t = c0; t < c0 + nCycles; ++t) {
+#pragma unroll 1
+    for (uint32_t r = 0; r < 2; ++r) {
+      const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
+      const uint32_t b = __ldg(ib + blockIdx.x), e = __ldg(ib + blockIdx.x + 1);
+      const long long tStart = clock64();
+      for (uint32_t i = b; i < e; ++i) {
+        const long long t0 = clock64();
+        const uint32_t item = __ldg(p.items + i);
+        evalItem<SPW, G>(p, item, vp, tab, t);
+        // per-partition clock64 profile (SimEval.cu:894-983): running mean of
+        // the useful ticks over cycles [100, 200) of group block 0
+        if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {
+          const uint32_t pid = item & 0xFFFFFu, pc = t - c0 - 100;
+          const long long useful = clock64() - t0;
+          p.profUseful[pid] = (p.profUseful[pid] * pc + useful) / (pc + 1);
+        }
+      }
+      if (r == 0 && (p.flags & kFlagDigest)) digestSlice<SPW>(p);
+      if (r == 1) {
+        if ((p.flags & kFlagStimulus) && t + 1 < c0 + nCycles) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
+        if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
+      }
+      if (!gridSync(p, gen)) return;
+      if ((p.flags & kFlagProfile) && threadIdx.x == 0 && t >= c0 + 100 && t < c0 + 200) {
+        const long long total = clock64() - tStart;
+        const uint32_t pc = t - c0 - 100;
+        for (uint32_t i = b; i < e; ++i) {
+          const uint32_t item = __ldg(p.items + i);
+          if ((item >> 20) != 0) continue;
+          const uint32_t pid = item & 0xFFFFFu;
+          p.profTotal[pid] = (p.profTotal[pid] * pc + total) / (pc + 1);
+        }
+      }
+    }
+    if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
+  }
+}
+
+// ---- state utilities -----------------------------------------------------------
+template <int SPW>
+__global__ void initStateKernel(const KParams p) {
+  const size_t n = size_t(p.regSlots) * p.gpad;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t v = p.initRegs[i / p.gpad];
+    p.regs[i] = SPW == 8 ? rep8(v) : v;
+  }
+  const size_t ne = size_t(p.exgSlots) * p.gpad;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < ne; i += size_t(gridDim.x) * blockDim.x) p.exg[i] = 0;
+}
+
+// Digest of one pool per stream: sum of mix64(i << 8 | v_i).
+__global__ void memDigestKernel(const uint8_t *__restrict__ mems, unsigned long long stride, uint32_t size,
+                                uint32_t nStreams, unsigned long long *__restrict__ out) {
+  const uint32_t s = blockIdx.y;
+  if (s >= nStreams) return;
+  const uint8_t *m = mems + s * stride;
+  unsigned long long acc = 0;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < size; i += size_t(gridDim.x) * blockDim.x)
+    acc += dmix64((unsigned long long)i << 8 | m[i]);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if ((threadIdx.x & 31u) == 0) atomicAdd(out + s, acc);
+}
+
+template <int SPW>
+__global__ void regDigestKernel(const uint32_t *__restrict__ regs, uint32_t slots, uint32_t gpad, uint32_t nStreams,
+                                unsigned long long *__restrict__ out) {
+  const uint32_t g = blockIdx.y;
+  unsigned long long acc[SPW];
+#pragma unroll
+  for (int k = 0; k < SPW; ++k) acc[k] = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+    const uint32_t w = regs[size_t(i) * gpad + g];
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) acc[k] += dmix64((unsigned long long)i << 8 | nib(w, k));
+  }
+#pragma unroll
+  for (int k = 0; k < SPW; ++k) {
+    unsigned long long a = acc[k];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    const uint32_t s = g * SPW + k;
+    if ((threadIdx.x & 31u) == 0 && s < nStreams) atomicAdd(out + s, a);
+  }
+}
+
+// nibble k of every register word of group g <-> one byte per register
+__global__ void gatherRegsKernel(const uint32_t *__restrict__ regs, uint32_t slots, uint32_t gpad, uint32_t g,
+                                 uint32_t k, uint8_t *__restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x)
+    out[i] = uint8_t(nib(regs[size_t(i) * gpad + g], k));
+}
+
+__global__ void scatterRegsKernel(uint32_t *__restrict__ regs, uint32_t slots, uint32_t gpad, uint32_t g, uint32_t k,
+                                  const uint8_t *__restrict__ in) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+    uint32_t *w = regs + size_t(i) * gpad + g;
+    *w = (*w & ~(15u << (4 * k))) | ((uint32_t(in[i]) & 15u) << (4 * k));
+  }
+}
+
+// Writes nibbles (id, value) of one stream.
+__global__ void pokeRegsKernel(uint32_t *__restrict__ regs, uint32_t gpad, uint32_t g, uint32_t k,
+                               const uint32_t *__restrict__ ids, const uint8_t *__restrict__ vals, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t *w = regs + size_t(ids[i]) * gpad + g;
+    *w = (*w & ~(15u << (4 * k))) | ((uint32_t(vals[i]) & 15u) << (4 * k));
+  }
+}
+
+template <int SPW, int G>
+void *cycleKernelPtr() {
+  return reinterpret_cast<void *>(&cycleKernel<SPW, G>);
+}
+
+}  // namespace
+
+void *cycleKernelFor(int spw, int G) {
+  if (spw == 1) return cycleKernelPtr<1, 1>();
+  if (G == 4) return cycleKernelPtr<8, 4>();
+  if (G == 2) return cycleKernelPtr<8, 2>();
+  return cycleKernelPtr<8, 1>();
+}
+
+cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint32_t n) {
+  void *fn = cycleKernelFor(c.spw, c.G);
+  KParams pp = p;
+  void *args[] = {&pp, &c0, &n};
+  return cudaLaunchCooperativeKernel(fn, dim3(c.blocks), dim3(c.threads), args, c.smem, c.stream);
+}
+
+cudaError_t launchInitState(int spw, const KParams &p, cudaStream_t st) {
+  const size_t n = size_t(p.regSlots) * p.gpad;
+  const uint32_t blocks = uint32_t(std::min<size_t>(4096, (n + 255) / 256 + 1));
+  if (spw == 8)
+    initStateKernel<8><<<blocks, 256, 0, st>>>(p);
+  else
+    initStateKernel<1><<<blocks, 256, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launchRegDigest(int spw, const uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t nStreams,
+                            unsigned long long *out, cudaStream_t st) {
+  dim3 grid(std::max<uint32_t>(1, std::min<uint32_t>(64, (slots + 255) / 256)), gpad);
+  if (spw == 8)
+    regDigestKernel<8><<<grid, 256, 0, st>>>(regs, slots, gpad, nStreams, out);
+  else
+    regDigestKernel<1><<<grid, 256, 0, st>>>(regs, slots, gpad, nStreams, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchMemDigest(const uint8_t *mems, unsigned long long stride, uint32_t size, uint32_t nStreams,
+                            unsigned long long *out, cudaStream_t st) {
+  if (size == 0 || nStreams == 0) return cudaSuccess;
+  dim3 grid(std::max<uint32_t>(1, std::min<uint32_t>(1024, (size + 255) / 256)), nStreams);
+  memDigestKernel<<<grid, 256, 0, st>>>(mems, stride, size, nStreams, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchGatherRegs(const uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t g, uint32_t k, uint8_t *out,
+                             cudaStream_t st) {
+  gatherRegsKernel<<<std::max<uint32_t>(1, std::min<uint32_t>(1024, (slots + 255) / 256)), 256, 0, st>>>(regs, slots, gpad, g, k, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchScatterRegs(uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t g, uint32_t k, const uint8_t *in,
+                              cudaStream_t st) {
+  scatterRegsKernel<<<std::max<uint32_t>(1, std::min<uint32_t>(1024, (slots + 255) / 256)), 256, 0, st>>>(regs, slots, gpad, g, k, in);
+  return cudaGetLastError();
+}
+
+cudaError_t launchPokeRegs(uint32_t *regs, uint32_t gpad, uint32_t g, uint32_t k, const uint32_t *ids,
+                           const uint8_t *vals, uint32_t n, cudaStream_t st) {
+  if (!n) return cudaSuccess;
+  pokeRegsKernel<<<std::max<uint32_t>(1, std::min<uint32_t>(1024, (n + 255) / 256)), 256, 0, st>>>(regs, gpad, g, k, ids, vals, n);
+  return cudaGetLastError();
+}
+
+}  // namespace tgs

@@ -1,0 +1,125 @@
+// Device image of a design: the GB300 layout the cycle kernel executes.
+//
+// It replaces the reference's per-partition pointer tables
+// (SimPartitionPtrs / SimMPartLevelInfo / SimMicroPartNetlistHeader,
+// src/SimEval.cu:61-65,152-187) with one 16-byte aligned word array per
+// design, offsets instead of pointers, lane-major op words (lane l of a warp
+// loads word l of every level, one 128-byte transaction per warp), and a
+// static warp schedule per exec level in place of the shared-memory atomic
+// work queue (SimEval.cu:818-843).
+//
+// Values: every value-pool slot, register and exchange entry is one 32-bit
+// word holding the nibbles of 8 streams (stream k of a group in bits
+// 4k..4k+3).  The reference stores one stream, one nibble per byte.
+#pragma once
+#include <cstdint>
+
+namespace tgs {
+
+// Micro-partition kinds (first header word, bits 0..1).
+enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
+
+// Header word: kind | lanes(6) << 2 | nMid(8) << 8 | nWB(6) << 16 | nTop(6) << 24.
+// LUT micro-partition words after the 4-word header (all lane-major):
+//   top:  2 * W words, lane l: [lutIndex | op0 << 16, op1 | op2 << 16] (zero for idle lanes)
+//   mid:  nMid * W words, the reference's packed middle-level op (zero = move of immediate 0)
+//   wb :  W words, lane l: shuffleId | result << 16
+// Special micro-partitions: header, then per lane fixed-size records:
+//   VecRead (5 words): vecBase | vecLength << 16, offset | isConst << 16,
+//                      idx0 | idx1 << 16, idx2 | idx3 << 16, outRange | result << 16
+//   VecOp   (3 words): vec1 | vec2 << 16, vecLength | opName << 16 | isV1V2Const << 24, result
+//   MemRead (4 words): memBase lo, memBase hi | multiWriter << 31, en | addrVec << 16, result
+constexpr uint32_t kMPHeaderWords = 4;
+constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;
+
+struct PartDesc {
+  uint32_t vpSlots;      // value-pool slots (multiple of 4)
+  uint32_t l0Count;      // L0 reads
+  uint32_t l0Off;        // word offset: src[l0Count], then dst packed two per word
+  uint32_t l0Exchange;   // 1: L0 reads the exchange pool, 0: registers
+  uint32_t nLevels;      // exec levels
+  uint32_t schedOff;     // word offset of the warp schedule (see below)
+  uint32_t copyKind;     // 0 none, 1 register pool, 2 exchange pool
+  uint32_t copySrc;      // first source slot (dat & ~3)
+  uint32_t copyDst;      // first destination entry (reg/exchange & ~3)
+  uint32_t copySlots;    // 4 * ((count + 3) / 4)
+  uint32_t memWCount, memWOff;   // 4 words per op: memBase lo, hi | multi << 31, addrVec | dat << 16, en
+  uint32_t printCount, printOff; // 1 word per op: en | msg << 16
+  uint32_t stopCount, stopOff;   // 1 word per op: en
+  uint32_t constOff, constLen;   // byte offset / length in the const-vector byte array
+  uint32_t region;
+  uint32_t pad[5];
+};
+static_assert(sizeof(PartDesc) == 96, "PartDesc size");
+
+// Warp schedule of a partition (at PartDesc::schedOff), for NW warps:
+//   per exec level: 1 word flags (bit0: block barrier before the level),
+//                   NW + 1 words: prefix offsets into the unit list of the level,
+//                   then the unit list: word offsets of micro-partitions.
+// Levels are stored back to back; level k's record starts where k-1's ends.
+
+// Kernel parameters (passed by value).
+struct KParams {
+  const uint32_t *net;        // design words
+  const uint32_t *sched;      // warp schedules (PartDesc::schedOff)
+  const PartDesc *parts;
+  const uint8_t *constVec;
+  const uint8_t *lutTable;    // 4642 entries, padded to 4656
+  const uint32_t *items;      // per region: list of (part | groupBlock << 20)
+  const uint32_t *itemBegin;  // [2][nBlocks + 1] prefix offsets into items per block
+  uint32_t *regs;             // [regSlots][gpad] words
+  uint32_t *exg;              // [exgSlots][gpad] words
+  uint8_t *mems;              // [nStreams][memStride]
+  const uint8_t *initRegs;    // [regSlots] initial nibbles
+  const uint8_t *initMems;    // [memPoolSize]
+  uint32_t *stop;             // [nStreams] sticky stop flags
+  uint32_t *stopCycle;        // [nStreams] first stop cycle
+  uint32_t *err;              // device error word (kErr*)
+  uint32_t *errInfo;          // [4] detail of the first error
+  uint32_t *barrier;          // [2]: arrival counter, generation
+  uint32_t *realCycles;
+  unsigned long long *digAcc; // [nStreams] per-cycle digest accumulators
+  unsigned long long *roll;   // [nStreams] rolling digests
+  unsigned long long *cycDig; // [nStreams][cycStride] or null
+  long long *profUseful;      // [nParts] or null
+  long long *profTotal;       // [nParts] or null
+  // stimulus
+  const uint32_t *stimReg;
+  const uint8_t *stimBits;
+  const uint16_t *stimToggle;
+  const unsigned long long *streamSeed;  // [nStreams]
+  uint32_t nStim;
+  uint32_t regSlots, exgSlots, memPoolSize;
+  unsigned long long memStride;
+  uint32_t nStreams, gpad;    // streams, padded 8-stream groups
+  uint32_t groupsPerItem;
+  uint32_t maxVpSlots;
+  uint32_t nBlocks;
+  uint32_t nParts;
+  uint32_t cycStride;
+  uint32_t enablePrint;
+  uint32_t flags;             // kFlag*
+  uint32_t printDiag;         // reference-style first-stop diagnostics (single stream)
+  unsigned long long timeoutNs;
+  const char *const *printMsgs;
+  uint32_t nPrintMsgs;
+  uint32_t pad0;
+};
+
+enum : uint32_t {
+  kFlagStimulus = 1u,   // apply the stimulus before every cycle
+  kFlagDigest = 2u,     // per-cycle register digests (rolling / per-cycle array)
+  kFlagProfile = 4u,    // per-partition clock64 profile (free-running)
+  kFlagCountCycles = 8u // advance realCycles (free-running launches only, SimEval.cu:985-989)
+};
+
+enum : uint32_t {
+  kErrNone = 0,
+  kErrTimeout = 1,      // grid barrier wait ran out of budget
+  kErrMemRange = 2,     // memory read/write beyond the pool
+  kErrBadOp = 3,        // unknown micro-partition kind
+};
+
+constexpr uint32_t kLutTablePadded = 4656;  // 4642 rounded up to 16 bytes
+
+}  // namespace tgs

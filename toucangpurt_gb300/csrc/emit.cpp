@@ -1,0 +1,361 @@
+// Design -> device image, and the static schedule.
+//
+// The image replaces the reference's copy_netlist_to_gpu / copyMicroPartToNetlist
+// (src/SimEval.cu:69-148,1114-1343): instead of per-level pointer arrays and
+// a magic-tagged byte stream per micro-partition, every micro-partition is a
+// 16-byte aligned record of lane-major 32-bit words (devimage.h), and the
+// order in which warps take micro-partitions is fixed here instead of by the
+// shared-memory atomic counter of SimEval.cu:818-843.  The schedule is the
+// only thing the greedy and the learned cost models change: values do not
+// depend on it for designs that pass the static checks.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <vector>
+
+#include "emit.h"
+
+namespace tgs {
+
+using namespace toucanGPUSim;
+
+namespace {
+
+void align4(std::vector<uint32_t> &v) {
+  while (v.size() % 4) v.push_back(0);
+}
+
+uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f) {
+  uint32_t W = uint32_t(m.topLevel.size());
+  for (auto &l : m.middleLevels) W = std::max<uint32_t>(W, uint32_t(l.size()));
+  W = std::max<uint32_t>(W, uint32_t(m.lastLevel.size()));
+  W = std::max<uint32_t>(W, 1);
+  uint32_t nMid = uint32_t(m.middleLevels.size());
+  align4(net);
+  uint32_t off = uint32_t(net.size());
+  net.push_back(kMPLut | (W << 2) | (nMid << 8) | (uint32_t(m.lastLevel.size()) << 16) |
+                (uint32_t(m.topLevel.size()) << 24));
+  net.push_back(0);
+  net.push_back(0);
+  net.push_back(0);
+  for (uint32_t l = 0; l < W; ++l) {
+    if (l < m.topLevel.size()) {
+      const auto &o = m.topLevel[l];
+      net.push_back(uint32_t(o.lutIndex) | (uint32_t(o.op0) << 16));
+      net.push_back(uint32_t(o.op1) | (uint32_t(o.op2) << 16));
+      f.ops += 1;
+      f.nops += o.lutIndex == 0;
+      f.vpReads += (o.op0 >= 16) + (o.op1 >= 16) + (o.op2 >= 16);
+      f.threeOp += o.op0 >= 16;
+    } else {
+      net.push_back(0);
+      net.push_back(0);
+    }
+  }
+  for (auto &lvl : m.middleLevels)
+    for (uint32_t l = 0; l < W; ++l) {
+      uint32_t w = l < lvl.size() ? lvl[l].getPacked() : 0u;
+      net.push_back(w);
+      if (l < lvl.size()) {
+        f.ops += 1;
+        f.nops += (w >> 18) == 0;
+        f.threeOp += ((w >> 12) & 63) >= 32;
+      }
+    }
+  for (uint32_t l = 0; l < W; ++l) {
+    if (l < m.lastLevel.size())
+      net.push_back(uint32_t(m.lastLevel[l].shuffleId) | (uint32_t(m.lastLevel[l].result) << 16));
+    else
+      net.push_back(0);
+  }
+  f.kind = kMPLut;
+  f.lanes = W;
+  f.depth = nMid + 1;
+  f.writes = uint32_t(m.lastLevel.size());
+  return off;
+}
+
+uint32_t emitSpecial(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f) {
+  align4(net);
+  uint32_t off = uint32_t(net.size());
+  if (!m.vecRead.empty()) {
+    uint32_t n = uint32_t(m.vecRead.size());
+    net.push_back(kMPVecRead | (n << 2));
+    net.push_back(0); net.push_back(0); net.push_back(0);
+    for (auto &o : m.vecRead) {
+      net.push_back(uint32_t(o.vecBase) | (uint32_t(o.vecLength) << 16));
+      net.push_back(uint32_t(o.offset) | (uint32_t(o.isConstVec ? 1 : 0) << 16));
+      net.push_back(uint32_t(o.index0) | (uint32_t(o.index1) << 16));
+      net.push_back(uint32_t(o.index2) | (uint32_t(o.index3) << 16));
+      net.push_back(uint32_t(o.outRangeValue) | (uint32_t(o.result) << 16));
+    }
+    f.kind = kMPVecRead;
+    f.lanes = n;
+    f.ops = n;
+    f.vpReads = 5 * n;
+    f.writes = n;
+  } else if (!m.vecArithAndLogic.empty()) {
+    uint32_t n = uint32_t(m.vecArithAndLogic.size());
+    net.push_back(kMPVecOp | (n << 2));
+    net.push_back(0); net.push_back(0); net.push_back(0);
+    for (auto &o : m.vecArithAndLogic) {
+      net.push_back(uint32_t(o.vec1Base) | (uint32_t(o.vec2Base) << 16));
+      net.push_back(uint32_t(o.vecLength) | (uint32_t(o.opName) << 16) | (uint32_t(o.isV1V2Const) << 24));
+      net.push_back(uint32_t(o.result));
+      f.vecNibbles += o.vecLength;
+      f.writes += o.opName <= VEC_ARITH_MUL ? o.vecLength : 1;
+    }
+    f.kind = kMPVecOp;
+    f.lanes = n;
+    f.ops = n;
+    f.vpReads = 2 * f.vecNibbles;
+  } else {
+    uint32_t n = uint32_t(m.memRead.size());
+    net.push_back(kMPMemRead | (n << 2));
+    net.push_back(0); net.push_back(0); net.push_back(0);
+    for (auto &o : m.memRead) {
+      net.push_back(uint32_t(o.memBase & 0xFFFFFFFFu));
+      net.push_back(uint32_t((o.memBase >> 32) & 0x7FFFFFFFu) | (o.hasMultipleWriter ? 0x80000000u : 0u));
+      net.push_back(uint32_t(o.en) | (uint32_t(o.addrVec) << 16));
+      net.push_back(uint32_t(o.result));
+    }
+    f.kind = kMPMemRead;
+    f.lanes = n;
+    f.ops = n;
+    f.memPorts = n;
+    f.vpReads = 9 * n;
+    f.writes = n;
+  }
+  f.depth = 1;
+  return off;
+}
+
+// Slots read / written by a micro-partition (for barrier placement).
+void accessOf(const CGMicroPartInfo &m, std::vector<uint32_t> &rd, std::vector<uint32_t> &wr) {
+  if (m.isLUTPart) {
+    for (auto &o : m.topLevel) {
+      if (o.op0 >= 16) rd.push_back(o.op0);
+      if (o.op1 >= 16) rd.push_back(o.op1);
+      if (o.op2 >= 16) rd.push_back(o.op2);
+    }
+    for (auto &w : m.lastLevel) wr.push_back(w.result);
+  } else if (!m.vecRead.empty()) {
+    for (auto &o : m.vecRead) {
+      for (uint16_t s : {o.index0, o.index1, o.index2, o.index3})
+        if (s >= 16) rd.push_back(s);
+      if (o.outRangeValue >= 16) rd.push_back(o.outRangeValue);
+      if (!o.isConstVec)
+        for (uint32_t i = 0; i < o.vecLength; ++i) rd.push_back(o.vecBase + i);
+      wr.push_back(o.result);
+    }
+  } else if (!m.vecArithAndLogic.empty()) {
+    for (auto &o : m.vecArithAndLogic) {
+      if (!(o.isV1V2Const & 2))
+        for (uint32_t i = 0; i < o.vecLength; ++i) rd.push_back(o.vec1Base + i);
+      if (!(o.isV1V2Const & 1))
+        for (uint32_t i = 0; i < o.vecLength; ++i) rd.push_back(o.vec2Base + i);
+      uint32_t n = o.opName <= VEC_ARITH_MUL ? o.vecLength : 1;
+      for (uint32_t i = 0; i < n; ++i) wr.push_back(uint16_t(o.result + i));
+    }
+  } else {
+    for (auto &o : m.memRead) {
+      if (o.en >= 16) rd.push_back(o.en);
+      for (uint32_t j = 0; j < 8; ++j) rd.push_back(o.addrVec + j);
+      if (o.en != 0) wr.push_back(o.result);
+    }
+  }
+}
+
+}  // namespace
+
+void buildImage(const SimDesignInfo &d, DeviceImage &img) {
+  img = DeviceImage();
+  img.parts.resize(d.parts.size());
+  img.mp.resize(d.parts.size());
+  img.partRegion.assign(d.parts.size(), 0);
+  for (size_t r = 0; r < d.regionPartitionIds.size(); ++r)
+    for (uint32_t id : d.regionPartitionIds[r]) img.partRegion[id] = uint32_t(r);
+  auto &net = img.net;
+  for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
+    const SimPartitionInfo &p = d.parts[pid];
+    PartDesc &pd = img.parts[pid];
+    std::memset(&pd, 0, sizeof(pd));
+    pd.vpSlots = (std::max<uint32_t>(p.valuePoolSize, 16) + 3) & ~3u;
+    pd.region = img.partRegion[pid];
+    // L0 reads
+    bool exg = !p.ops_l0_exchangeRead.empty();
+    pd.l0Exchange = exg ? 1 : 0;
+    pd.l0Count = uint32_t(exg ? p.ops_l0_exchangeRead.size() : p.ops_l0_regRead.size());
+    align4(net);
+    pd.l0Off = uint32_t(net.size());
+    for (uint32_t i = 0; i < pd.l0Count; ++i) net.push_back(exg ? p.ops_l0_exchangeRead[i].exchange : p.ops_l0_regRead[i].reg);
+    for (uint32_t i = 0; i < pd.l0Count; i += 2) {
+      auto dst = [&](uint32_t k) -> uint32_t {
+        if (k >= pd.l0Count) return 0;
+        return exg ? p.ops_l0_exchangeRead[k].result : p.ops_l0_regRead[k].result;
+      };
+      net.push_back(dst(i) | (dst(i + 1) << 16));
+    }
+    // micro-partitions
+    pd.nLevels = uint32_t(p.exec_mParts.size());
+    img.mp[pid].resize(pd.nLevels);
+    for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
+      for (const auto &m : p.exec_mParts[lv]) {
+        MPartRef ref;
+        ref.feat.partLevels = pd.nLevels;
+        ref.off = m.isLUTPart ? emitLut(m, net, ref.feat) : emitSpecial(m, net, ref.feat);
+        accessOf(m, ref.reads, ref.writes);
+        std::sort(ref.reads.begin(), ref.reads.end());
+        ref.reads.erase(std::unique(ref.reads.begin(), ref.reads.end()), ref.reads.end());
+        ref.feat.fanIn = uint32_t(ref.reads.size());
+        img.mp[pid][lv].push_back(std::move(ref));
+      }
+    }
+    // last level
+    if (p.op_last_exchangeWrite.count != 0) {
+      auto op = lastLevelExchangeOp(p);
+      pd.copyKind = 2;
+      pd.copySrc = op.dat & ~3u;
+      pd.copyDst = op.exchange & ~3u;
+      pd.copySlots = (uint32_t(op.count) + 3) / 4 * 4;
+    } else {
+      if (p.op_last_regWrite.count != 0) {
+        pd.copyKind = 1;
+        pd.copySrc = p.op_last_regWrite.dat & ~3u;
+        pd.copyDst = p.op_last_regWrite.reg & ~3u;
+        pd.copySlots = (uint32_t(p.op_last_regWrite.count) + 3) / 4 * 4;
+      }
+      align4(net);
+      pd.memWCount = uint32_t(p.ops_last_memWrite.size());
+      pd.memWOff = uint32_t(net.size());
+      for (auto &w : p.ops_last_memWrite) {
+        net.push_back(uint32_t(w.memBase & 0xFFFFFFFFu));
+        net.push_back(uint32_t((w.memBase >> 32) & 0x7FFFFFFFu) | (w.hasMultipleWriter ? 0x80000000u : 0u));
+        net.push_back(uint32_t(w.addrVec) | (uint32_t(w.dat) << 16));
+        net.push_back(uint32_t(w.en));
+      }
+      pd.printCount = uint32_t(p.ops_last_print.size());
+      pd.printOff = uint32_t(net.size());
+      for (auto &pr : p.ops_last_print) net.push_back(uint32_t(pr.en) | (uint32_t(pr.msg) << 16));
+      pd.stopCount = uint32_t(p.ops_last_stop.size());
+      pd.stopOff = uint32_t(net.size());
+      for (auto &st : p.ops_last_stop) net.push_back(uint32_t(st.en));
+    }
+    pd.constOff = uint32_t(img.constVec.size());
+    pd.constLen = uint32_t(p.constVecPool.size());
+    img.constVec.insert(img.constVec.end(), p.constVecPool.begin(), p.constVecPool.end());
+    while (img.constVec.size() % 16) img.constVec.push_back(0);
+    img.maxVpSlots = std::max(img.maxVpSlots, pd.vpSlots);
+  }
+  align4(net);
+  if (net.empty()) net.resize(4, 0);
+  if (img.constVec.empty()) img.constVec.resize(16, 0);
+}
+
+// Greedy gate-count cost of a micro-partition (the fallback cost model).
+float gateCost(const MPartFeat &f) { return float(std::max<uint32_t>(1, f.ops)); }
+
+void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const std::vector<std::vector<std::vector<float>>> *cost,
+                   uint32_t nBlocks, uint32_t nGroupBlocks, Schedule &out) {
+  out = Schedule();
+  out.NW = NW;
+  out.partCost.assign(d.parts.size(), 0.0);
+  auto &sw = out.words;
+  for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
+    PartDesc &pd = img.parts[pid];
+    pd.schedOff = uint32_t(sw.size());
+    double total = 0;
+    // barrier placement: hazards since the last block barrier, tracked per slot
+    std::vector<int32_t> lastWriter(pd.vpSlots + 64, -1);  // warp of last write since the barrier
+    std::vector<uint32_t> readersMask(pd.vpSlots + 64, 0);  // warps that read since the barrier
+    std::vector<uint32_t> touched;
+    for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
+      const auto &mps = img.mp[pid][lv];
+      // LPT: largest cost first onto the least loaded warp
+      std::vector<uint32_t> order(mps.size());
+      std::iota(order.begin(), order.end(), 0u);
+      auto costOf = [&](uint32_t i) { return cost ? (*cost)[pid][lv][i] : gateCost(mps[i].feat); };
+      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return costOf(a) > costOf(b); });
+      std::vector<double> load(NW, 0.0);
+      std::vector<std::vector<uint32_t>> perWarp(NW);
+      for (uint32_t i : order) {
+        uint32_t w = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
+        load[w] += costOf(i);
+        perWarp[w].push_back(i);
+      }
+      total += *std::max_element(load.begin(), load.end());
+      // does this level need a block barrier first?
+      bool need = lv == 0;
+      if (!need) {
+        for (uint32_t w = 0; w < NW && !need; ++w)
+          for (uint32_t i : perWarp[w]) {
+            for (uint32_t s : mps[i].reads)
+              if (lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) { need = true; break; }
+            if (need) break;
+            for (uint32_t s : mps[i].writes)
+              if ((lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) || (readersMask[s] & ~(1u << w))) { need = true; break; }
+            if (need) break;
+          }
+      }
+      if (need) {
+        for (uint32_t s : touched) { lastWriter[s] = -1; readersMask[s] = 0; }
+        touched.clear();
+        out.barriers++;
+      }
+      for (uint32_t w = 0; w < NW; ++w)
+        for (uint32_t i : perWarp[w]) {
+          for (uint32_t s : mps[i].reads) { readersMask[s] |= 1u << w; touched.push_back(s); }
+          for (uint32_t s : mps[i].writes) { lastWriter[s] = int32_t(w); touched.push_back(s); }
+        }
+      out.levels++;
+      sw.push_back(need ? 1u : 0u);
+      uint32_t acc = 0;
+      for (uint32_t w = 0; w < NW; ++w) {
+        sw.push_back(acc);
+        acc += uint32_t(perWarp[w].size());
+      }
+      sw.push_back(acc);
+      for (uint32_t w = 0; w < NW; ++w)
+        for (uint32_t i : perWarp[w]) sw.push_back(mps[i].off);
+    }
+    // L0 and last level scale with their op counts spread over the block
+    total += double(pd.l0Count + pd.copySlots + 8 * pd.memWCount) / double(32 * NW) + 1.0;
+    out.partCost[pid] = total;
+  }
+  if (sw.empty()) sw.push_back(0);
+
+  // items (partition, group block) onto blocks, per region, LPT by cost
+  out.items.clear();
+  out.itemBegin.assign(2 * (nBlocks + 1), 0);
+  for (uint32_t r = 0; r < 2; ++r) {
+    std::vector<std::pair<double, uint32_t>> it;
+    for (uint32_t pid : d.regionPartitionIds[r])
+      for (uint32_t gb = 0; gb < nGroupBlocks; ++gb) it.push_back({out.partCost[pid], pid | (gb << 20)});
+    std::stable_sort(it.begin(), it.end(), [](auto &a, auto &b) { return a.first > b.first; });
+    using E = std::pair<double, uint32_t>;
+    std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
+    for (uint32_t b = 0; b < nBlocks; ++b) pq.push({0.0, b});
+    std::vector<std::vector<uint32_t>> perBlock(nBlocks);
+    double mk = 0;
+    for (auto &e : it) {
+      auto top = pq.top();
+      pq.pop();
+      perBlock[top.second].push_back(e.second);
+      top.first += e.first;
+      mk = std::max(mk, top.first);
+      pq.push(top);
+    }
+    out.makespan[r] = mk;
+    uint32_t base = uint32_t(out.items.size());
+    for (uint32_t b = 0; b < nBlocks; ++b) {
+      out.itemBegin[r * (nBlocks + 1) + b] = base;
+      for (uint32_t x : perBlock[b]) out.items.push_back(x);
+      base = uint32_t(out.items.size());
+    }
+    out.itemBegin[r * (nBlocks + 1) + nBlocks] = base;
+  }
+  if (out.items.empty()) out.items.push_back(0);
+}
+
+}  // namespace tgs

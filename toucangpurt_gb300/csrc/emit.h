@@ -1,0 +1,61 @@
+// Host-side device image and schedule (see emit.cpp).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "devimage.h"
+#include "tgs_internal.h"
+
+namespace tgs {
+
+// Structural features of one micro-partition: the inputs of the learned cost
+// model and of the gate-count fallback.
+struct MPartFeat {
+  uint32_t kind = 0;        // kMPLut / kMPVecRead / kMPVecOp / kMPMemRead
+  uint32_t lanes = 0;       // widest level
+  uint32_t depth = 0;       // levels (top + middle)
+  uint32_t ops = 0;         // op slots (LUT + moves, or special lanes)
+  uint32_t nops = 0;        // moves
+  uint32_t threeOp = 0;     // ops with a non-immediate op0
+  uint32_t vpReads = 0;     // value-pool operand reads
+  uint32_t writes = 0;      // slots written
+  uint32_t memPorts = 0;
+  uint32_t vecNibbles = 0;
+  uint32_t fanIn = 0;       // distinct slots read
+  uint32_t fanOut = 0;      // later readers of its outputs
+  uint32_t partLevels = 0;  // exec levels of its partition
+};
+
+struct MPartRef {
+  uint32_t off = 0;  // word offset in DeviceImage::net
+  MPartFeat feat;
+  std::vector<uint32_t> reads, writes;
+};
+
+struct DeviceImage {
+  std::vector<uint32_t> net;
+  std::vector<PartDesc> parts;
+  std::vector<uint8_t> constVec;
+  std::vector<uint32_t> partRegion;
+  std::vector<std::vector<std::vector<MPartRef>>> mp;  // [part][level][i]
+  uint32_t maxVpSlots = 0;
+};
+
+struct Schedule {
+  uint32_t NW = 0;
+  std::vector<uint32_t> words;      // per-partition warp schedules (PartDesc::schedOff)
+  std::vector<uint32_t> items;      // (part | groupBlock << 20) per region and block
+  std::vector<uint32_t> itemBegin;  // [2][nBlocks + 1]
+  std::vector<double> partCost;
+  double makespan[2] = {0, 0};
+  uint64_t barriers = 0, levels = 0;
+};
+
+void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img);
+// cost: optional [part][level][mpart] predicted cost; null = gate count.
+void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW,
+                   const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,
+                   Schedule &out);
+float gateCost(const MPartFeat &f);
+
+}  // namespace tgs

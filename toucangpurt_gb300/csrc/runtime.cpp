@@ -1,0 +1,913 @@
+// Host runtime and C ABI (include/toucan_gb300.h).
+//
+// Replaces the reference host path: ToucanSimulator::init / setupGPU /
+// eval / eval_free_running (src/ToucanSim.cu:16-267), copy_netlist_to_gpu and
+// the register I/O (src/SimEval.cu:1058-1343).  Differences by design: a
+// handle instead of process-global device state, every allocation freed by
+// tgs_destroy, status codes instead of exit(), and many streams per handle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "emit.h"
+#include "kernels.h"
+#include "learned.h"
+#include "tgs_internal.h"
+
+using namespace toucanGPUSim;
+
+namespace tgs {
+
+namespace {
+thread_local std::string gLastError;
+}
+
+void setLastError(const std::string &m) { gLastError = m; }
+
+std::vector<uint8_t> readFileBytes(const std::string &path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error(TGS_ERR_IO, "cannot open " + path);
+  return std::vector<uint8_t>(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+}
+
+#define TGS_CUDA(call)                                                                                     \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess) throw ::tgs::Error(TGS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Device buffer owned by a handle.
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    free();
+    if (count == 0) count = 1;
+    TGS_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T *src, size_t count, cudaStream_t s) {
+    if (count > n) alloc(count);
+    if (count) TGS_CUDA(cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T> &v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { free(); }
+};
+
+}  // namespace tgs
+
+struct tgs_sim {
+  tgs_options opt{};
+  SimDesignInfo design;
+  SimDebugInfo symbols;
+  tgs::ValidateInfo vinfo;
+  tgs::DeviceImage img;
+  tgs::Schedule sched;
+  bool loaded = false;
+  int device = -1;
+  cudaDeviceProp props{};
+  cudaStream_t stream = nullptr;
+  bool enablePrint = false;
+  uint64_t cycleCnt = 0;
+  uint64_t streamCycles = 0;  // batch bookkeeping
+
+  // launch configuration
+  tgs::LaunchCfg lc;
+  uint32_t spw = 1, groups = 1, gpad = 1, nStreams = 1, regSlots = 4, exgSlots = 4;
+  unsigned long long memStride = 16;
+
+  // device memory
+  tgs::DBuf<uint32_t> net, schedW, items, itemBegin, regs, exg, stop, stopCycle, err, errInfo, barrier, realCycles, stimReg;
+  tgs::DBuf<tgs::PartDesc> parts;
+  tgs::DBuf<uint8_t> constVec, lutTable, mems, initRegs, initMems, stimBits;
+  tgs::DBuf<uint16_t> stimToggle;
+  tgs::DBuf<unsigned long long> digAcc, roll, cycDig, seeds, outA, outB;
+  tgs::DBuf<long long> profU, profT;
+  tgs::DBuf<char *> msgPtrs;
+  std::vector<tgs::DBuf<char>> msgs;
+  tgs::DBuf<uint32_t> ioIds;
+  tgs::DBuf<uint8_t> ioBytes;
+  tgs::KParams kp{};
+  // learned cost model (optional)
+  std::unique_ptr<tgs::CostModel> model;
+
+  ~tgs_sim() {
+    if (device >= 0) cudaSetDevice(device);
+    for (auto &m : msgs) m.free();
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace tgs {
+namespace {
+
+void checkDeviceError(tgs_sim *h) {
+  uint32_t info[4] = {0, 0, 0, 0};
+  TGS_CUDA(cudaMemcpy(info, h->errInfo.p, sizeof(info), cudaMemcpyDeviceToHost));
+  uint32_t code = 0;
+  TGS_CUDA(cudaMemcpy(&code, h->err.p, sizeof(code), cudaMemcpyDeviceToHost));
+  if (code == kErrNone) return;
+  uint32_t zero[4] = {0, 0, 0, 0};
+  TGS_CUDA(cudaMemcpy(h->err.p, zero, sizeof(uint32_t), cudaMemcpyHostToDevice));
+  TGS_CUDA(cudaMemcpy(h->errInfo.p, zero, sizeof(zero), cudaMemcpyHostToDevice));
+  char buf[256];
+  if (code == kErrTimeout) {
+    std::snprintf(buf, sizeof buf, "device barrier wait ran out of its budget (block %u, generation %u)", info[1], info[2]);
+    throw Error(TGS_ERR_TIMEOUT, buf);
+  }
+  if (code == kErrMemRange) {
+    unsigned long long idx = (unsigned long long)info[1] | ((unsigned long long)info[2] << 32);
+    std::snprintf(buf, sizeof buf, "memory access at index %llu beyond memPool (stream %u)", idx, info[3]);
+    throw Error(TGS_ERR_DEVICE_FAULT, buf);
+  }
+  std::snprintf(buf, sizeof buf, "device check failed (code %u)", code);
+  throw Error(TGS_ERR_DEVICE_FAULT, buf);
+}
+
+void fillParams(tgs_sim *h) {
+  KParams &p = h->kp;
+  std::memset(&p, 0, sizeof(p));
+  p.net = h->net.p;
+  p.sched = h->schedW.p;
+  p.parts = h->parts.p;
+  p.constVec = h->constVec.p;
+  p.lutTable = h->lutTable.p;
+  p.items = h->items.p;
+  p.itemBegin = h->itemBegin.p;
+  p.regs = h->regs.p;
+  p.exg = h->exg.p;
+  p.mems = h->mems.p;
+  p.initRegs = h->initRegs.p;
+  p.initMems = h->initMems.p;
+  p.stop = h->stop.p;
+  p.stopCycle = h->stopCycle.p;
+  p.err = h->err.p;
+  p.errInfo = h->errInfo.p;
+  p.barrier = h->barrier.p;
+  p.realCycles = h->realCycles.p;
+  p.digAcc = h->digAcc.p;
+  p.roll = h->roll.p;
+  p.cycDig = nullptr;
+  p.profUseful = h->profU.p;
+  p.profTotal = h->profT.p;
+  p.streamSeed = h->seeds.p;
+  p.regSlots = h->regSlots;
+  p.exgSlots = h->exgSlots;
+  p.memPoolSize = h->design.memPoolSize;
+  p.memStride = h->memStride;
+  p.nStreams = h->nStreams;
+  p.gpad = h->gpad;
+  p.groupsPerItem = uint32_t(h->lc.G);
+  p.maxVpSlots = h->img.maxVpSlots;
+  p.nBlocks = h->lc.blocks;
+  p.nParts = uint32_t(h->design.parts.size());
+  p.enablePrint = h->enablePrint ? 1 : 0;
+  p.printDiag = h->nStreams == 1 ? 1 : 0;
+  p.timeoutNs = (unsigned long long)std::max<uint32_t>(1, h->opt.barrier_timeout_ms) * 1000000ull;
+  p.printMsgs = h->msgPtrs.p;
+  p.nPrintMsgs = uint32_t(h->msgs.size());
+}
+
+// Launch shape, schedule and per-stream state for the current options.
+void configure(tgs_sim *h) {
+  const tgs_options &o = h->opt;
+  h->nStreams = std::max<uint32_t>(1, o.n_streams);
+  h->spw = h->nStreams == 1 ? 1 : 8;
+  h->groups = (h->nStreams + h->spw - 1) / h->spw;
+  int G = 1;
+  if (h->spw == 8) {
+    G = int(o.groups_per_item ? o.groups_per_item : 4);
+    if (G != 1 && G != 2 && G != 4) throw Error(TGS_ERR_ARG, "groups_per_item must be 1, 2 or 4");
+    while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
+  }
+  h->gpad = (h->groups + G - 1) / G * G;
+  uint32_t NW = o.warps_per_block ? o.warps_per_block : 8;
+  if (NW != 4 && NW != 8 && NW != 16 && NW != 32) throw Error(TGS_ERR_ARG, "warps_per_block must be 4, 8, 16 or 32");
+  h->lc.spw = int(h->spw);
+  h->lc.G = G;
+  h->lc.threads = NW * 32;
+  h->lc.smem = kLutTablePadded + size_t(h->img.maxVpSlots) * size_t(G) * 4;
+  h->lc.stream = h->stream;
+  void *fn = cycleKernelFor(int(h->spw), G);
+  if (h->lc.smem > size_t(h->props.sharedMemPerBlockOptin))
+    throw Error(TGS_ERR_RESOURCES, "value pool of " + std::to_string(h->img.maxVpSlots) + " slots x " + std::to_string(G) +
+                                       " groups needs " + std::to_string(h->lc.smem) + " B of shared memory; lower groups_per_item");
+  TGS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
+  int perSM = 0;
+  TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, int(h->lc.threads), h->lc.smem));
+  if (perSM <= 0) throw Error(TGS_ERR_RESOURCES, "no block of the cycle kernel fits on an SM with this configuration");
+  if (o.blocks_per_sm) perSM = std::min<int>(perSM, int(o.blocks_per_sm));
+  const uint32_t nGB = h->gpad / uint32_t(G);
+  size_t maxItems = 1;
+  for (auto &r : h->design.regionPartitionIds) maxItems = std::max(maxItems, r.size() * nGB);
+  h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
+
+  // schedule (greedy gate count or learned cost)
+  std::vector<std::vector<std::vector<float>>> cost;
+  const std::vector<std::vector<std::vector<float>>> *costPtr = nullptr;
+  if (o.schedule == TGS_SCHED_LEARNED && h->model && h->model->trained()) {
+    h->model->predictAll(h->img, cost);
+    costPtr = &cost;
+  }
+  buildSchedule(h->design, h->img, NW, costPtr, h->lc.blocks, nGB, h->sched);
+  h->parts.upload(h->img.parts, h->stream);
+  h->schedW.upload(h->sched.words, h->stream);
+  h->items.upload(h->sched.items, h->stream);
+  h->itemBegin.upload(h->sched.itemBegin, h->stream);
+
+  // per-stream state
+  h->regSlots = std::max<uint32_t>(4, (h->design.regPoolSize + 3) & ~3u);
+  h->exgSlots = std::max<uint32_t>(4, (h->design.exchangePoolSize + 3) & ~3u);
+  h->memStride = std::max<unsigned long long>(16, (h->design.memPoolSize + 15ull) & ~15ull);
+  h->regs.alloc(size_t(h->regSlots) * h->gpad);
+  h->exg.alloc(size_t(h->exgSlots) * h->gpad);
+  h->mems.alloc(size_t(h->memStride) * h->nStreams);
+  h->stop.alloc(h->nStreams);
+  h->stopCycle.alloc(h->nStreams);
+  h->digAcc.alloc(h->nStreams);
+  h->roll.alloc(h->nStreams);
+  h->seeds.alloc(h->nStreams);
+  h->outA.alloc(h->nStreams);
+  h->outB.alloc(h->nStreams);
+  fillParams(h);
+}
+
+void resetState(tgs_sim *h) {
+  TGS_CUDA(launchInitState(int(h->spw), h->kp, h->stream));
+  for (uint32_t s = 0; s < h->nStreams; ++s)
+    TGS_CUDA(cudaMemcpyAsync(h->mems.p + size_t(s) * h->memStride, h->initMems.p, h->design.memPoolSize,
+                             cudaMemcpyDeviceToDevice, h->stream));
+  TGS_CUDA(cudaMemsetAsync(h->stop.p, 0, h->nStreams * sizeof(uint32_t), h->stream));
+  TGS_CUDA(cudaMemsetAsync(h->stopCycle.p, 0xFF, h->nStreams * sizeof(uint32_t), h->stream));
+  TGS_CUDA(cudaMemsetAsync(h->realCycles.p, 0, sizeof(uint32_t), h->stream));
+  TGS_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+void setupDevice(tgs_sim *h, int gpu) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw Error(TGS_ERR_NO_DEVICE, "no CUDA device available");
+  if (gpu < 0 || gpu >= n) throw Error(TGS_ERR_NO_DEVICE, "gpu id " + std::to_string(gpu) + " out of range");
+  TGS_CUDA(cudaSetDevice(gpu));
+  TGS_CUDA(cudaGetDeviceProperties(&h->props, gpu));
+  // sm_103a code only (the reference requires cc >= 7.0, ToucanSim.cu:34-43)
+  if (h->props.major != 10) throw Error(TGS_ERR_NO_DEVICE, std::string("this build targets sm_103a; found ") + h->props.name);
+  if (!h->props.cooperativeLaunch) throw Error(TGS_ERR_NO_DEVICE, "GPU does not support cooperative launch");
+  h->device = gpu;
+  if (!h->stream) TGS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+}
+
+void upload(tgs_sim *h) {
+  cudaStream_t s = h->stream;
+  buildImage(h->design, h->img);
+  h->net.upload(h->img.net, s);
+  h->constVec.upload(h->img.constVec, s);
+  std::vector<uint8_t> lut(kLutTablePadded, 0);
+  std::memcpy(lut.data(), h->design.lut.data(), std::min<size_t>(h->design.lut.size(), kLutSize));
+  h->lutTable.upload(lut, s);
+  std::vector<uint8_t> ir(std::max<uint32_t>(4, (h->design.regPoolSize + 3) & ~3u), 0);
+  std::memcpy(ir.data(), h->design.regPool.data(), h->design.regPool.size());
+  h->initRegs.upload(ir, s);
+  h->initMems.alloc(std::max<size_t>(16, h->design.memPool.size()));
+  if (!h->design.memPool.empty())
+    TGS_CUDA(cudaMemcpyAsync(h->initMems.p, h->design.memPool.data(), h->design.memPool.size(), cudaMemcpyHostToDevice, s));
+  h->err.alloc(1);
+  h->errInfo.alloc(4);
+  h->barrier.alloc(2);
+  h->realCycles.alloc(1);
+  TGS_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(uint32_t), s));
+  TGS_CUDA(cudaMemsetAsync(h->errInfo.p, 0, 4 * sizeof(uint32_t), s));
+  h->profU.alloc(h->design.parts.size());
+  h->profT.alloc(h->design.parts.size());
+  // print messages (copy_netlist_to_gpu, SimEval.cu:1313-1326)
+  for (auto &m : h->msgs) m.free();
+  h->msgs.clear();
+  h->msgs.resize(h->design.printMsgs.size());
+  std::vector<char *> ptrs;
+  for (size_t i = 0; i < h->design.printMsgs.size(); ++i) {
+    const std::string &str = h->design.printMsgs[i];
+    h->msgs[i].upload(str.c_str(), str.size() + 1, s);
+    ptrs.push_back(h->msgs[i].p);
+  }
+  if (ptrs.empty()) ptrs.push_back(nullptr);
+  h->msgPtrs.upload(ptrs, s);
+  TGS_CUDA(cudaStreamSynchronize(s));
+}
+
+void initCommon(tgs_sim *h, int gpu, const uint8_t *design, size_t dn, const uint8_t *sym, size_t sn, bool randomize,
+                bool print) {
+  h->loaded = false;
+  h->design = SimDesignInfo();
+  h->symbols = SimDebugInfo();
+  parseDesign(design, dn, h->design);
+  if (sym) parseSymbols(sym, sn, h->symbols);
+  h->design.Init();
+  if (randomize) h->design.Randomize(0, h->symbols);
+  h->vinfo = ValidateInfo();
+  if (h->opt.validate) h->vinfo = validateDesign(h->design, &h->symbols);
+  setupDevice(h, gpu);
+  h->enablePrint = print;
+  upload(h);
+  configure(h);
+  resetState(h);
+  h->cycleCnt = 0;
+  h->loaded = true;
+}
+
+void requireLoaded(tgs_sim *h) {
+  if (!h) throw Error(TGS_ERR_ARG, "null handle");
+  if (!h->loaded) throw Error(TGS_ERR_STATE, "simulator not initialised");
+  TGS_CUDA(cudaSetDevice(h->device));
+}
+
+void runCycles(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
+  if (n == 0) return;
+  h->kp.flags = flags;
+  TGS_CUDA(cudaMemsetAsync(h->barrier.p, 0, 2 * sizeof(uint32_t), h->stream));
+  TGS_CUDA(launchCycles(h->lc, h->kp, c0, n));
+}
+
+int stopFlag(tgs_sim *h) {
+  std::vector<uint32_t> st(h->nStreams);
+  TGS_CUDA(cudaMemcpy(st.data(), h->stop.p, st.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  for (uint32_t v : st)
+    if (v) return 1;
+  return 0;
+}
+
+const std::vector<std::tuple<uint32_t, uint32_t>> &regLocs(tgs_sim *h, const char *name) {
+  if (!name) throw Error(TGS_ERR_ARG, "null register name");
+  auto it = h->symbols.regDebugInfo.find(name);
+  if (it == h->symbols.regDebugInfo.end()) throw Error(TGS_ERR_NOT_FOUND, std::string("unknown register ") + name);
+  if (it->second.size() > 16) throw Error(TGS_ERR_RANGE, std::string("register wider than 64 bits: ") + name);
+  return it->second;
+}
+
+void streamPos(tgs_sim *h, uint32_t s, uint32_t &g, uint32_t &k) {
+  if (s >= h->nStreams) throw Error(TGS_ERR_ARG, "stream index out of range");
+  g = s / h->spw;
+  k = s % h->spw;
+}
+
+// write_reg_to_gpu (SimEval.cu:1072-1081): least significant nibble to the
+// last listed id; all nibbles written in one kernel.
+void setRegister(tgs_sim *h, uint32_t s, const char *name, uint64_t value) {
+  const auto &locs = regLocs(h, name);
+  std::vector<uint32_t> ids;
+  std::vector<uint8_t> vals;
+  uint64_t v = value;
+  for (auto it = locs.rbegin(); it != locs.rend(); ++it) {
+    ids.push_back(std::get<0>(*it));
+    vals.push_back(uint8_t(v & 0xF));
+    v >>= 4;
+  }
+  if (v != 0) throw Error(TGS_ERR_RANGE, std::string("value wider than register ") + name);
+  for (uint32_t id : ids)
+    if (id >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "register id beyond regPool");
+  uint32_t g, k;
+  streamPos(h, s, g, k);
+  h->ioIds.upload(ids, h->stream);
+  h->ioBytes.upload(vals, h->stream);
+  TGS_CUDA(launchPokeRegs(h->regs.p, h->gpad, g, k, h->ioIds.p, h->ioBytes.p, uint32_t(ids.size()), h->stream));
+  TGS_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+// read_reg_from_gpu (SimEval.cu:1058-1069): most significant nibble first.
+uint64_t readRegister(tgs_sim *h, uint32_t s, const char *name) {
+  const auto &locs = regLocs(h, name);
+  uint32_t g, k;
+  streamPos(h, s, g, k);
+  uint64_t r = 0;
+  for (auto &l : locs) {
+    uint32_t id = std::get<0>(l), w = 0;
+    if (id >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "register id beyond regPool");
+    TGS_CUDA(cudaMemcpy(&w, h->regs.p + size_t(id) * h->gpad + g, 4, cudaMemcpyDeviceToHost));
+    r = (r << 4) | ((w >> (4 * k)) & 0xF);
+  }
+  return r;
+}
+
+template <typename F>
+int guard(F f) {
+  try {
+    f();
+    return TGS_OK;
+  } catch (const Error &e) {
+    setLastError(e.what());
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    setLastError("host out of memory");
+    return TGS_ERR_RESOURCES;
+  } catch (const std::exception &e) {
+    setLastError(e.what());
+    return TGS_ERR_ARG;
+  }
+}
+
+}  // namespace
+
+// ---- batch runs -------------------------------------------------------------
+void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res);
+
+}  // namespace tgs
+
+using namespace tgs;
+
+extern "C" {
+
+const char *tgs_last_error(void) { return gLastError.c_str(); }
+const char *tgs_version(void) { return "toucan-gb300 0.1 (sm_103a)"; }
+
+int tgs_create(tgs_sim **out) {
+  return guard([&] {
+    if (!out) throw Error(TGS_ERR_ARG, "null output pointer");
+    *out = new tgs_sim();
+    tgs_default_options(&(*out)->opt);
+  });
+}
+
+int tgs_destroy(tgs_sim *h) {
+  return guard([&] { delete h; });
+}
+
+int tgs_default_options(tgs_options *o) {
+  return guard([&] {
+    if (!o) throw Error(TGS_ERR_ARG, "null options");
+    std::memset(o, 0, sizeof(*o));
+    o->n_streams = 1;
+    o->warps_per_block = 8;
+    o->groups_per_item = 4;
+    o->blocks_per_sm = 0;
+    o->schedule = TGS_SCHED_GREEDY;
+    o->mode = TGS_MODE_PERSISTENT;
+    o->barrier_timeout_ms = 5000;
+    o->validate = 1;
+    o->resident_netlist = 0;
+  });
+}
+
+int tgs_set_options(tgs_sim *h, const tgs_options *o) {
+  return guard([&] {
+    if (!h || !o) throw Error(TGS_ERR_ARG, "null argument");
+    h->opt = *o;
+    if (h->loaded) {
+      TGS_CUDA(cudaSetDevice(h->device));
+      configure(h);
+      resetState(h);
+    }
+  });
+}
+
+int tgs_get_options(const tgs_sim *h, tgs_options *o) {
+  return guard([&] {
+    if (!h || !o) throw Error(TGS_ERR_ARG, "null argument");
+    *o = h->opt;
+  });
+}
+
+int tgs_init(tgs_sim *h, int gpu_id, const char *design_path, const char *symbol_path, int randomize, int enable_print) {
+  return guard([&] {
+    if (!h || !design_path) throw Error(TGS_ERR_ARG, "null argument");
+    auto d = readFileBytes(design_path);
+    std::vector<uint8_t> s;
+    if (symbol_path) s = readFileBytes(symbol_path);
+    initCommon(h, gpu_id, d.data(), d.size(), symbol_path ? s.data() : nullptr, s.size(), randomize != 0, enable_print != 0);
+  });
+}
+
+int tgs_init_from_memory(tgs_sim *h, int gpu_id, const void *design, size_t dn, const void *symbols, size_t sn,
+                         int randomize, int enable_print) {
+  return guard([&] {
+    if (!h || !design) throw Error(TGS_ERR_ARG, "null argument");
+    initCommon(h, gpu_id, static_cast<const uint8_t *>(design), dn, static_cast<const uint8_t *>(symbols), sn,
+               randomize != 0, enable_print != 0);
+  });
+}
+
+int tgs_eval(tgs_sim *h, int *stop) {
+  return guard([&] {
+    requireLoaded(h);
+    runCycles(h, uint32_t(h->cycleCnt), 1, 0);
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    checkDeviceError(h);
+    h->cycleCnt += 1;
+    if (stop) *stop = stopFlag(h);
+  });
+}
+
+int tgs_eval_free_running(tgs_sim *h, uint32_t cycles, int *stop) {
+  return guard([&] {
+    requireLoaded(h);
+    TGS_CUDA(cudaMemsetAsync(h->profU.p, 0, h->profU.n * sizeof(long long), h->stream));
+    TGS_CUDA(cudaMemsetAsync(h->profT.p, 0, h->profT.n * sizeof(long long), h->stream));
+    runCycles(h, uint32_t(h->cycleCnt), cycles, kFlagCountCycles | kFlagProfile);
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    checkDeviceError(h);
+    h->cycleCnt += cycles;
+    if (stop) *stop = stopFlag(h);
+  });
+}
+
+int tgs_set_register(tgs_sim *h, const char *name, uint64_t value) {
+  return guard([&] { requireLoaded(h); setRegister(h, 0, name, value); });
+}
+int tgs_read_register(tgs_sim *h, const char *name, uint64_t *value) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!value) throw Error(TGS_ERR_ARG, "null output");
+    *value = readRegister(h, 0, name);
+  });
+}
+int tgs_set_register_stream(tgs_sim *h, uint32_t s, const char *name, uint64_t value) {
+  return guard([&] { requireLoaded(h); setRegister(h, s, name, value); });
+}
+int tgs_read_register_stream(tgs_sim *h, uint32_t s, const char *name, uint64_t *value) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!value) throw Error(TGS_ERR_ARG, "null output");
+    *value = readRegister(h, s, name);
+  });
+}
+
+int tgs_read_signal(tgs_sim *h, const char *name, uint64_t *value) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!name || !value) throw Error(TGS_ERR_ARG, "null argument");
+    if (!h->symbols.signalDebugInfo.count(name)) throw Error(TGS_ERR_NOT_FOUND, std::string("unknown signal ") + name);
+    *value = UINT64_MAX;
+  });
+}
+
+int tgs_get_real_cycles(tgs_sim *h, uint32_t *c) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!c) throw Error(TGS_ERR_ARG, "null output");
+    TGS_CUDA(cudaMemcpy(c, h->realCycles.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  });
+}
+int tgs_get_cycle_cnt(tgs_sim *h, uint64_t *c) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!c) throw Error(TGS_ERR_ARG, "null output");
+    *c = h->cycleCnt;
+  });
+}
+int tgs_set_enable_print(tgs_sim *h, int en) {
+  return guard([&] {
+    requireLoaded(h);
+    h->enablePrint = en != 0;
+    h->kp.enablePrint = en ? 1 : 0;
+  });
+}
+int tgs_get_eval_done(tgs_sim *h, int *stop) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!stop) throw Error(TGS_ERR_ARG, "null output");
+    *stop = stopFlag(h);
+  });
+}
+
+int tgs_copy_profile_data(tgs_sim *h, int64_t *useful, int64_t *total, size_t count) {
+  return guard([&] {
+    requireLoaded(h);
+    if (count > h->design.parts.size()) throw Error(TGS_ERR_RANGE, "count beyond partition count");
+    if (useful) TGS_CUDA(cudaMemcpy(useful, h->profU.p, count * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (total) TGS_CUDA(cudaMemcpy(total, h->profT.p, count * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  });
+}
+
+int tgs_get_pool_sizes(const tgs_sim *h, uint32_t *r, uint32_t *m, uint32_t *e) {
+  return guard([&] {
+    if (!h || !h->loaded) throw Error(TGS_ERR_STATE, "simulator not initialised");
+    if (r) *r = h->design.regPoolSize;
+    if (m) *m = h->design.memPoolSize;
+    if (e) *e = h->design.exchangePoolSize;
+  });
+}
+
+int tgs_read_reg_pool(tgs_sim *h, uint32_t s, uint8_t *out, size_t bytes) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!out || bytes != h->design.regPoolSize) throw Error(TGS_ERR_ARG, "buffer must hold regPoolSize bytes");
+    uint32_t g, k;
+    streamPos(h, s, g, k);
+    h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
+    TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+    TGS_CUDA(cudaMemcpyAsync(out, h->ioBytes.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int tgs_write_reg_pool(tgs_sim *h, uint32_t s, const uint8_t *in, size_t bytes) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!in || bytes != h->design.regPoolSize) throw Error(TGS_ERR_ARG, "buffer must hold regPoolSize bytes");
+    uint32_t g, k;
+    streamPos(h, s, g, k);
+    std::vector<uint8_t> buf(h->regSlots, 0);
+    std::memcpy(buf.data(), in, bytes);
+    // keep the padding slots as they are: read them first
+    std::vector<uint8_t> cur(h->regSlots);
+    h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
+    TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+    TGS_CUDA(cudaMemcpyAsync(cur.data(), h->ioBytes.p, h->regSlots, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t i = bytes; i < h->regSlots; ++i) buf[i] = cur[i];
+    h->ioBytes.upload(buf, h->stream);
+    TGS_CUDA(launchScatterRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int tgs_read_mem_pool(tgs_sim *h, uint32_t s, uint8_t *out, size_t bytes) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!out || bytes != h->design.memPoolSize) throw Error(TGS_ERR_ARG, "buffer must hold memPoolSize bytes");
+    if (s >= h->nStreams) throw Error(TGS_ERR_ARG, "stream index out of range");
+    TGS_CUDA(cudaMemcpy(out, h->mems.p + size_t(s) * h->memStride, bytes, cudaMemcpyDeviceToHost));
+  });
+}
+
+int tgs_write_mem_pool(tgs_sim *h, uint32_t s, const uint8_t *in, size_t bytes) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!in || bytes != h->design.memPoolSize) throw Error(TGS_ERR_ARG, "buffer must hold memPoolSize bytes");
+    if (s >= h->nStreams) throw Error(TGS_ERR_ARG, "stream index out of range");
+    TGS_CUDA(cudaMemcpy(h->mems.p + size_t(s) * h->memStride, in, bytes, cudaMemcpyHostToDevice));
+  });
+}
+
+int tgs_state_digest(tgs_sim *h, uint32_t s, uint64_t *rd, uint64_t *md) {
+  return guard([&] {
+    requireLoaded(h);
+    if (s >= h->nStreams) throw Error(TGS_ERR_ARG, "stream index out of range");
+    TGS_CUDA(cudaMemsetAsync(h->outA.p, 0, h->nStreams * 8, h->stream));
+    TGS_CUDA(cudaMemsetAsync(h->outB.p, 0, h->nStreams * 8, h->stream));
+    TGS_CUDA(launchRegDigest(int(h->spw), h->regs.p, h->design.regPoolSize, h->gpad, h->nStreams, h->outA.p, h->stream));
+    TGS_CUDA(launchMemDigest(h->mems.p, h->memStride, h->design.memPoolSize, h->nStreams, h->outB.p, h->stream));
+    unsigned long long a = 0, b = 0;
+    TGS_CUDA(cudaMemcpyAsync(&a, h->outA.p + s, 8, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaMemcpyAsync(&b, h->outB.p + s, 8, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    if (rd) *rd = a;
+    if (md) *md = b;
+  });
+}
+
+int tgs_reset_state(tgs_sim *h) {
+  return guard([&] {
+    requireLoaded(h);
+    resetState(h);
+    h->cycleCnt = 0;
+  });
+}
+
+int tgs_batch_run(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
+  return guard([&] {
+    requireLoaded(h);
+    batchRun(h, job, res);
+  });
+}
+
+int tgs_default_gen_config(tgs_gen_config *c) {
+  return guard([&] {
+    if (!c) throw Error(TGS_ERR_ARG, "null config");
+    std::memset(c, 0, sizeof(*c));
+    c->seed = 1;
+    c->n_lut = 4096;
+    c->levels = 16;
+    c->operands = 2;
+    c->ff_bits = 512;
+    c->pi_bits = 32;
+    c->n_mems = 1;
+    c->mem_depth = 1024;
+    c->mem_width = 32;
+    c->mem_read_ports = 1;
+    c->mem_write_ports = 1;
+    c->vec_nibbles = 8;
+    c->max_fanout = 4096;
+    c->luts_per_part = 2048;
+    c->mpart_width = 32;
+    c->cone_depth = 1;
+  });
+}
+
+int tgs_generate(const tgs_gen_config *cfg, const char *design_path, const char *symbol_path, tgs_gen_info *info) {
+  return guard([&] {
+    if (!cfg || !design_path) throw Error(TGS_ERR_ARG, "null argument");
+    SimDesignInfo d;
+    SimDebugInfo s;
+    generateDesign(*cfg, d, s, info);
+    {
+      std::ofstream o(design_path, std::ios::binary);
+      if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + design_path);
+      serializeSimDesignInfo(o, d);
+      if (!o) throw Error(TGS_ERR_IO, std::string("write failed: ") + design_path);
+    }
+    if (symbol_path) {
+      std::ofstream o(symbol_path, std::ios::binary);
+      if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + symbol_path);
+      serializeSimDebugInfo(o, s);
+    }
+  });
+}
+
+int tgs_validate_file(const char *design_path, const char *symbol_path, uint64_t *lut_ops) {
+  return guard([&] {
+    if (!design_path) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(design_path);
+    SimDesignInfo d;
+    SimDebugInfo s;
+    parseDesign(bytes.data(), bytes.size(), d);
+    if (symbol_path) {
+      auto sb = readFileBytes(symbol_path);
+      parseSymbols(sb.data(), sb.size(), s);
+    }
+    d.Init();
+    auto vi = validateDesign(d, symbol_path ? &s : nullptr);
+    if (lut_ops) *lut_ops = vi.lutOps;
+  });
+}
+
+}  // extern "C"
+
+namespace tgs {
+
+// Streams of a job run from the initial state for cycles[s] cycles each, all
+// resident at once (the current slot count must hold the job).
+void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
+  if (!job || !job->cycles || job->n_streams == 0) throw Error(TGS_ERR_ARG, "empty batch");
+  const uint32_t n = job->n_streams;
+  uint32_t cyc = job->cycles[0];
+  for (uint32_t s = 1; s < n; ++s)
+    if (job->cycles[s] != cyc) throw Error(TGS_ERR_ARG, "streams of unequal length need resident slots < n_streams");
+  if (h->opt.n_streams != n) {
+    h->opt.n_streams = n;
+    configure(h);
+  }
+  const tgs_stimulus *st = job->stim;
+  uint32_t flags = 0;
+  if (st && st->n_inputs) {
+    flags |= kFlagStimulus;
+    // primary inputs must not be targets of a partition's register copy
+    for (auto &pd : h->img.parts)
+      if (pd.copyKind == 1)
+        for (uint32_t i = 0; i < st->n_inputs; ++i)
+          if (st->reg[i] >= pd.copyDst && st->reg[i] < pd.copyDst + pd.copySlots)
+            throw Error(TGS_ERR_ARG, "stimulus register " + std::to_string(st->reg[i]) + " is written by the design");
+    for (uint32_t i = 0; i < st->n_inputs; ++i) {
+      if (st->reg[i] >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "stimulus register beyond regPool");
+      if (st->bits[i] < 1 || st->bits[i] > 4) throw Error(TGS_ERR_RANGE, "stimulus bit width outside 1..4");
+    }
+    h->stimReg.upload(st->reg, st->n_inputs, h->stream);
+    h->stimBits.upload(st->bits, st->n_inputs, h->stream);
+    if (st->toggle) h->stimToggle.upload(st->toggle, st->n_inputs, h->stream);
+    std::vector<unsigned long long> seeds(n);
+    for (uint32_t s = 0; s < n; ++s) seeds[s] = mix64(st->base_seed ^ s);
+    h->seeds.upload(seeds, h->stream);
+  }
+  const bool wantDigest = (job->flags & (TGS_BATCH_CYCLE_DIGESTS | TGS_BATCH_ROLLING)) != 0;
+  if (wantDigest) flags |= kFlagDigest;
+  if (flags) {
+    // stimulus and digests run beside the regions: registers must be
+    // read-only in region 0 and unread in region 1
+    for (auto &pd : h->img.parts) {
+      if (pd.region == 0 && pd.copyKind == 1) throw Error(TGS_ERR_INVALID_DESIGN, "region 0 writes registers: stimulus/digest runs need region-0 register writes to be absent");
+      if (pd.region == 1 && pd.l0Exchange == 0 && pd.l0Count) throw Error(TGS_ERR_INVALID_DESIGN, "region 1 reads registers: stimulus/digest runs need region 1 to read only the exchange pool");
+    }
+  }
+  resetState(h);
+  fillParams(h);
+  KParams &p = h->kp;
+  p.nStim = st ? st->n_inputs : 0;
+  p.stimReg = h->stimReg.p;
+  p.stimBits = h->stimBits.p;
+  p.stimToggle = (st && st->toggle) ? h->stimToggle.p : nullptr;
+  p.streamSeed = h->seeds.p;
+  TGS_CUDA(cudaMemsetAsync(h->digAcc.p, 0, n * 8, h->stream));
+  TGS_CUDA(cudaMemsetAsync(h->roll.p, 0, n * 8, h->stream));
+  const bool perCycle = (job->flags & TGS_BATCH_CYCLE_DIGESTS) && res && res->cycle_digest && res->cycle_stride;
+  if (perCycle) {
+    h->cycDig.alloc(size_t(n) * res->cycle_stride);
+    TGS_CUDA(cudaMemsetAsync(h->cycDig.p, 0, size_t(n) * res->cycle_stride * 8, h->stream));
+    p.cycDig = h->cycDig.p;
+    p.cycStride = res->cycle_stride;
+  }
+  cudaEvent_t e0, e1;
+  TGS_CUDA(cudaEventCreate(&e0));
+  TGS_CUDA(cudaEventCreate(&e1));
+  TGS_CUDA(cudaEventRecord(e0, h->stream));
+  runCycles(h, 0, cyc, flags);
+  TGS_CUDA(cudaEventRecord(e1, h->stream));
+  TGS_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  TGS_CUDA(cudaStreamSynchronize(h->stream));
+  checkDeviceError(h);
+  h->cycleCnt = cyc;
+  if (!res) return;
+  res->device_ms = ms;
+  res->stream_cycles = uint64_t(cyc) * n;
+  res->launches = 1;
+  if (res->final_reg_digest || res->final_mem_digest) {
+    TGS_CUDA(cudaMemsetAsync(h->outA.p, 0, n * 8, h->stream));
+    TGS_CUDA(cudaMemsetAsync(h->outB.p, 0, n * 8, h->stream));
+    TGS_CUDA(launchRegDigest(int(h->spw), h->regs.p, h->design.regPoolSize, h->gpad, n, h->outA.p, h->stream));
+    TGS_CUDA(launchMemDigest(h->mems.p, h->memStride, h->design.memPoolSize, n, h->outB.p, h->stream));
+    if (res->final_reg_digest) TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outA.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (res->final_mem_digest) TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outB.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  }
+  if (res->rolling_digest) TGS_CUDA(cudaMemcpyAsync(res->rolling_digest, h->roll.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (perCycle)
+    TGS_CUDA(cudaMemcpyAsync(res->cycle_digest, h->cycDig.p, size_t(n) * res->cycle_stride * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (res->stop_cycle) TGS_CUDA(cudaMemcpyAsync(res->stop_cycle, h->stopCycle.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+  TGS_CUDA(cudaStreamSynchronize(h->stream));
+  if (res->final_regs || res->final_mems) {
+    std::vector<uint8_t> buf;
+    for (uint32_t s = 0; s < n; ++s) {
+      uint32_t g = s / h->spw, k = s % h->spw;
+      if (res->final_regs) {
+        h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
+        TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+        TGS_CUDA(cudaMemcpyAsync(res->final_regs + size_t(s) * h->design.regPoolSize, h->ioBytes.p,
+                                 h->design.regPoolSize, cudaMemcpyDeviceToHost, h->stream));
+        TGS_CUDA(cudaStreamSynchronize(h->stream));
+      }
+      if (res->final_mems)
+        TGS_CUDA(cudaMemcpy(res->final_mems + size_t(s) * h->design.memPoolSize, h->mems.p + size_t(s) * h->memStride,
+                            h->design.memPoolSize, cudaMemcpyDeviceToHost));
+    }
+  }
+}
+
+}  // namespace tgs
+
+namespace tgs {
+const SimDesignInfo &designOf(const tgs_sim *h) { return h->design; }
+const SimDebugInfo &symbolsOf(const tgs_sim *h) { return h->symbols; }
+}  // namespace tgs
+
+extern "C" int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *o) {
+  return guard([&] {
+    if (!h || !o) throw Error(TGS_ERR_ARG, "null argument");
+    if (!h->loaded) throw Error(TGS_ERR_STATE, "simulator not initialised");
+    std::memset(o, 0, sizeof(*o));
+    uint64_t slots = 0;
+    for (const auto &p : h->design.parts) {
+      o->l0_reg_reads += p.ops_l0_regRead.size();
+      o->l0_exg_reads += p.ops_l0_exchangeRead.size();
+      o->max_exec_levels = std::max<uint32_t>(o->max_exec_levels, uint32_t(p.exec_mParts.size()));
+      for (const auto &lvl : p.exec_mParts)
+        for (const auto &m : lvl) {
+          ++o->mparts;
+          slots += 1;  // header word
+          if (m.isLUTPart) {
+            for (const auto &t : m.topLevel) (t.lutIndex ? o->lut_ops : o->nop_ops)++;
+            for (const auto &l : m.middleLevels)
+              for (const auto &op : l) (op.lutIndex() ? o->lut_ops : o->nop_ops)++;
+            o->writeback_ops += m.lastLevel.size();
+          }
+          o->vec_read_ops += m.vecRead.size();
+          o->vec_ops += m.vecArithAndLogic.size();
+          o->mem_read_ops += m.memRead.size();
+        }
+      if (p.op_last_exchangeWrite.count) {
+        o->exg_copy_slots += (lastLevelExchangeOp(p).count + 3) / 4 * 4;
+      } else {
+        if (p.op_last_regWrite.count) o->reg_copy_slots += (p.op_last_regWrite.count + 3) / 4 * 4;
+        o->mem_write_ops += p.ops_last_memWrite.size();
+        o->print_ops += p.ops_last_print.size();
+        o->stop_ops += p.ops_last_stop.size();
+      }
+      slots += (p.op_last_regWrite.count || p.op_last_exchangeWrite.count) ? 1 : 0;
+    }
+    o->op_slots = slots + o->lut_ops + o->nop_ops + o->writeback_ops + o->l0_reg_reads + o->l0_exg_reads + o->mem_read_ops +
+                  o->mem_write_ops + o->vec_ops + o->vec_read_ops + o->print_ops + o->stop_ops;
+    o->partitions = uint32_t(h->design.parts.size());
+    o->max_value_pool = h->img.maxVpSlots;
+    o->blocks = h->lc.blocks;
+    o->threads = h->lc.threads;
+    o->groups_per_item = uint32_t(h->lc.G);
+    o->streams_per_word = h->spw;
+    o->block_barriers = h->sched.barriers;
+    o->exec_levels = h->sched.levels;
+    o->makespan[0] = h->sched.makespan[0];
+    o->makespan[1] = h->sched.makespan[1];
+  });
+}

@@ -1,0 +1,274 @@
+"""Python host API mirroring toucanGPUSim::ToucanSimulator (reference
+include/ToucanGPUSim.h:10-74), plus batched stimulus runs and the synthetic
+design generator.  Everything calls the C ABI (capi.py); nothing here
+evaluates a design.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import capi
+from .capi import check, lib
+
+
+def _ptr(a: np.ndarray | None, ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Simulator:
+    """One simulator handle (the reference's ToucanSimulator)."""
+
+    def __init__(self, **options):
+        self._h = C.c_void_p()
+        check(lib().tgs_create(C.byref(self._h)))
+        self._opt = capi.Options()
+        check(lib().tgs_default_options(C.byref(self._opt)))
+        self.set_options(**options)
+
+    # -- lifetime -------------------------------------------------------
+    def cleanup(self) -> None:
+        if self._h:
+            lib().tgs_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.cleanup()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.cleanup()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # -- options ----------------------------------------------------------
+    def set_options(self, **kw) -> None:
+        for k, v in kw.items():
+            if not hasattr(self._opt, k):
+                raise TypeError(f"unknown option {k}")
+            setattr(self._opt, k, int(v))
+        check(lib().tgs_set_options(self._h, C.byref(self._opt)))
+
+    def options(self) -> dict:
+        o = capi.Options()
+        check(lib().tgs_get_options(self._h, C.byref(o)))
+        return {f: getattr(o, f) for f, _ in capi.Options._fields_ if f != "reserved"}
+
+    # -- ToucanSimulator API ---------------------------------------------
+    def init(self, gpu_id: int, design_bin: str | Path, symbol_bin: str | Path | None, should_randomize: bool = False,
+             enable_print: bool = False) -> int:
+        """ToucanSimulator::init: 0 on success; raises TgsError otherwise."""
+        sym = str(symbol_bin).encode() if symbol_bin is not None else None
+        check(lib().tgs_init(self._h, gpu_id, str(design_bin).encode(), sym, int(should_randomize), int(enable_print)))
+        return 0
+
+    def eval(self) -> bool:
+        stop = C.c_int()
+        check(lib().tgs_eval(self._h, C.byref(stop)))
+        return bool(stop.value)
+
+    def eval_free_running(self, max_cycles: int) -> bool:
+        stop = C.c_int()
+        check(lib().tgs_eval_free_running(self._h, int(max_cycles), C.byref(stop)))
+        return bool(stop.value)
+
+    def set_register(self, name: str, value: int, stream: int = 0) -> None:
+        check(lib().tgs_set_register_stream(self._h, stream, name.encode(), int(value)))
+
+    def read_register(self, name: str, stream: int = 0) -> int:
+        v = C.c_uint64()
+        check(lib().tgs_read_register_stream(self._h, stream, name.encode(), C.byref(v)))
+        return v.value
+
+    # reference spellings
+    setRegister = set_register
+    readRegister = read_register
+
+    def read_signal(self, name: str) -> int:
+        v = C.c_uint64()
+        check(lib().tgs_read_signal(self._h, name.encode(), C.byref(v)))
+        return v.value
+
+    def real_cycles(self) -> int:
+        v = C.c_uint32()
+        check(lib().tgs_get_real_cycles(self._h, C.byref(v)))
+        return v.value
+
+    def cycle_cnt(self) -> int:
+        v = C.c_uint64()
+        check(lib().tgs_get_cycle_cnt(self._h, C.byref(v)))
+        return v.value
+
+    def eval_done(self) -> bool:
+        v = C.c_int()
+        check(lib().tgs_get_eval_done(self._h, C.byref(v)))
+        return bool(v.value)
+
+    def set_enable_print(self, on: bool) -> None:
+        check(lib().tgs_set_enable_print(self._h, int(on)))
+
+    def profile(self, n_parts: int) -> tuple[np.ndarray, np.ndarray]:
+        u = np.zeros(n_parts, np.int64)
+        t = np.zeros(n_parts, np.int64)
+        check(lib().tgs_copy_profile_data(self._h, _ptr(u, C.c_int64), _ptr(t, C.c_int64), n_parts))
+        return u, t
+
+    def design_stats(self) -> dict:
+        st = capi.DesignStats()
+        check(lib().tgs_get_design_stats(self._h, C.byref(st)))
+        d = {f: getattr(st, f) for f, _ in capi.DesignStats._fields_ if f not in ("reserved", "makespan")}
+        d["makespan"] = [st.makespan[0], st.makespan[1]]
+        return d
+
+    # -- state --------------------------------------------------------------
+    def pool_sizes(self) -> tuple[int, int, int]:
+        r, m, e = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().tgs_get_pool_sizes(self._h, C.byref(r), C.byref(m), C.byref(e)))
+        return r.value, m.value, e.value
+
+    def reg_pool(self, stream: int = 0) -> np.ndarray:
+        n = self.pool_sizes()[0]
+        a = np.zeros(n, np.uint8)
+        check(lib().tgs_read_reg_pool(self._h, stream, _ptr(a, C.c_uint8), n))
+        return a
+
+    def write_reg_pool(self, data: np.ndarray, stream: int = 0) -> None:
+        a = np.ascontiguousarray(data, np.uint8)
+        check(lib().tgs_write_reg_pool(self._h, stream, _ptr(a, C.c_uint8), a.size))
+
+    def mem_pool(self, stream: int = 0) -> np.ndarray:
+        n = self.pool_sizes()[1]
+        a = np.zeros(n, np.uint8)
+        check(lib().tgs_read_mem_pool(self._h, stream, _ptr(a, C.c_uint8), n))
+        return a
+
+    def write_mem_pool(self, data: np.ndarray, stream: int = 0) -> None:
+        a = np.ascontiguousarray(data, np.uint8)
+        check(lib().tgs_write_mem_pool(self._h, stream, _ptr(a, C.c_uint8), a.size))
+
+    def digest(self, stream: int = 0) -> tuple[int, int]:
+        r, m = C.c_uint64(), C.c_uint64()
+        check(lib().tgs_state_digest(self._h, stream, C.byref(r), C.byref(m)))
+        return r.value, m.value
+
+    def reset_state(self) -> None:
+        check(lib().tgs_reset_state(self._h))
+
+    # -- batched runs ---------------------------------------------------------
+    def batch_run(self, cycles, stim: "StimulusSpec | None" = None, *, cycle_digests: bool = False,
+                  rolling: bool = True, final_state: bool = False, slots: int = 0) -> "BatchOutput":
+        cyc = np.ascontiguousarray(cycles, np.uint32)
+        n = int(cyc.size)
+        out = BatchOutput(n)
+        stride = int(cyc.max()) if cycle_digests else 0
+        if cycle_digests:
+            out.cycle_digest = np.zeros((n, stride), np.uint64)
+        if final_state:
+            r, m, _ = self.pool_sizes()
+            out.final_regs = np.zeros((n, r), np.uint8)
+            out.final_mems = np.zeros((n, m), np.uint8)
+        flags = (capi.BATCH_CYCLE_DIGESTS if cycle_digests else 0) | (capi.BATCH_ROLLING if rolling else 0) | (
+            capi.BATCH_FINAL_STATE if final_state else 0)
+        st_ptr = C.cast(None, C.POINTER(capi.Stimulus))
+        keep = []
+        if stim is not None:
+            s = stim.to_c()
+            keep.append(s)
+            st_ptr = C.pointer(s[0])
+        job = capi.Batch(n, _ptr(cyc, C.c_uint32), st_ptr, flags, slots)
+        res = capi.BatchResult()
+        res.final_reg_digest = _ptr(out.final_reg_digest, C.c_uint64)
+        res.final_mem_digest = _ptr(out.final_mem_digest, C.c_uint64)
+        res.rolling_digest = _ptr(out.rolling_digest, C.c_uint64)
+        res.cycle_digest = _ptr(out.cycle_digest, C.c_uint64)
+        res.cycle_stride = stride
+        res.stop_cycle = _ptr(out.stop_cycle, C.c_uint32)
+        res.final_regs = _ptr(out.final_regs, C.c_uint8)
+        res.final_mems = _ptr(out.final_mems, C.c_uint8)
+        check(lib().tgs_batch_run(self._h, C.byref(job), C.byref(res)))
+        out.device_ms = res.device_ms
+        out.stream_cycles = res.stream_cycles
+        out.launches = res.launches
+        return out
+
+
+@dataclass
+class StimulusSpec:
+    """Primary inputs rewritten before every cycle (see tgs_stimulus)."""
+
+    base_seed: int
+    reg: np.ndarray
+    bits: np.ndarray
+    toggle: np.ndarray | None = None
+
+    def to_c(self):
+        reg = np.ascontiguousarray(self.reg, np.uint32)
+        bits = np.ascontiguousarray(self.bits, np.uint8)
+        tog = None if self.toggle is None else np.ascontiguousarray(self.toggle, np.uint16)
+        s = capi.Stimulus(self.base_seed, reg.size, _ptr(reg, C.c_uint32), _ptr(bits, C.c_uint8), _ptr(tog, C.c_uint16))
+        return (s, reg, bits, tog)
+
+
+@dataclass
+class BatchOutput:
+    n: int
+    final_reg_digest: np.ndarray = field(init=False)
+    final_mem_digest: np.ndarray = field(init=False)
+    rolling_digest: np.ndarray = field(init=False)
+    stop_cycle: np.ndarray = field(init=False)
+    cycle_digest: np.ndarray | None = None
+    final_regs: np.ndarray | None = None
+    final_mems: np.ndarray | None = None
+    device_ms: float = 0.0
+    stream_cycles: int = 0
+    launches: int = 0
+
+    def __post_init__(self):
+        self.final_reg_digest = np.zeros(self.n, np.uint64)
+        self.final_mem_digest = np.zeros(self.n, np.uint64)
+        self.rolling_digest = np.zeros(self.n, np.uint64)
+        self.stop_cycle = np.zeros(self.n, np.uint32)
+
+
+# ---- synthetic designs ---------------------------------------------------------
+def gen_config(**kw) -> capi.GenConfig:
+    c = capi.GenConfig()
+    check(lib().tgs_default_gen_config(C.byref(c)))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise TypeError(f"unknown generator field {k}")
+        setattr(c, k, v)
+    return c
+
+
+def generate(design_path: str | Path, symbol_path: str | Path, **kw) -> dict:
+    """Writes a seeded synthetic design (reference file format)."""
+    c = gen_config(**kw)
+    info = capi.GenInfo()
+    check(lib().tgs_generate(C.byref(c), str(design_path).encode(), str(symbol_path).encode(), C.byref(info)))
+    d = {f: getattr(info, f) for f, _ in capi.GenInfo._fields_ if f != "reserved"}
+    ids = np.zeros(info.n_pi_nibbles, np.uint32)
+    bits = np.zeros(info.n_pi_nibbles, np.uint8)
+    check(lib().tgs_gen_inputs(C.byref(c), _ptr(ids, C.c_uint32), _ptr(bits, C.c_uint8), info.n_pi_nibbles))
+    d["pi_ids"] = ids
+    d["pi_bits"] = bits
+    return d
+
+
+def validate_file(design_path, symbol_path=None) -> int:
+    n = C.c_uint64()
+    sym = str(symbol_path).encode() if symbol_path else None
+    check(lib().tgs_validate_file(str(design_path).encode(), sym, C.byref(n)))
+    return n.value
