@@ -50,6 +50,8 @@ def args_parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cycles", type=int, default=1)
     p.add_argument("--out", default="")
+    p.add_argument("--override", action="append", default=[],
+                   help="generator field override key=value (e.g. a smaller memory depth for profiling)")
     return p.parse_args()
 
 
@@ -140,11 +142,15 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def make_design(workload: str, workdir: Path, rank: int):
+def make_design(workload: str, workdir: Path, rank: int, overrides=()):
     from toucangpurt_gb300 import sim, workloads
 
+    ov = {}
+    for kv in overrides:
+        k, v = kv.split("=", 1)
+        ov[k] = float(v) if "." in v else int(v)
     dp, sp = workdir / f"{workload}.bin", workdir / f"{workload}.sym"
-    info = sim.generate(dp, sp, **workloads.design_config(workload))
+    info = sim.generate(dp, sp, **workloads.design_config(workload, **ov))
     return dp, sp, info
 
 
@@ -182,7 +188,7 @@ def run_reference(a, rank, ws):
     build.build()
     pyoracle.build()
     wd = Path(tempfile.mkdtemp(prefix="tgs_ref_"))
-    dp, sp, info = make_design(a.workload, wd, 0)
+    dp, sp, info = make_design(a.workload, wd, 0, a.override)
     streams = a.streams or workloads.RUNS[a.workload]["streams"]
     cyc = a.cpu_sample_cycles
     threads = os.cpu_count() or 1
@@ -219,7 +225,7 @@ def run_gb300(a, rank, ws):
     build.build()
     gpu = int(os.environ.get("LOCAL_RANK", "0"))
     wd = Path(tempfile.mkdtemp(prefix="tgs_bench_"))
-    dp, sp, info = make_design(a.workload, wd, rank)
+    dp, sp, info = make_design(a.workload, wd, rank, a.override)
     streams = a.streams or workloads.RUNS[a.workload]["streams"]
     cps = a.cycles_per_step or (200 if a.workload in ("largest", "learned") else 2000)
     schedule = 1 if a.schedule == "learned" else 0

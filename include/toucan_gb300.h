@@ -236,6 +236,16 @@ int tgs_generate(const tgs_gen_config *cfg, const char *design_path, const char 
  * (ids: [n], bits: [n]; n from tgs_gen_info.n_pi_nibbles). */
 int tgs_gen_inputs(const tgs_gen_config *cfg, uint32_t *ids, uint8_t *bits, uint32_t n);
 
+/* Host-only file utilities (no GPU needed).  tgs_resave_* load a file with
+ * this library's loader and write it back with its serializer (byte for byte
+ * the reference format).  tgs_initial_state: Init() and optionally
+ * Randomize(0) (reference src/SimInit.cpp:16-64) into caller buffers of
+ * regPoolSize / memPoolSize bytes. */
+int tgs_resave_design(const char *in_path, const char *out_path);
+int tgs_resave_symbols(const char *in_path, const char *out_path);
+int tgs_initial_state(const char *design_path, const char *symbol_path, int randomize, uint8_t *regs, size_t reg_bytes,
+                      uint8_t *mems, size_t mem_bytes);
+
 /* Static checks of a design file: the rules that make a design's values
  * independent of the schedule (def-before-use, no same-level slot conflicts,
  * word-aligned block copies, table bounds, nibble-valued tables). */

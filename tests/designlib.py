@@ -113,10 +113,13 @@ class Design:
     parts: list = field(default_factory=list)
     regions: list = field(default_factory=lambda: [[], []])
     msgs: list = field(default_factory=list)
+    reg_init: bytes = b""   # initial regPool contents (Init() keeps them, SimInit.cpp:16-26)
+    mem_init: bytes = b""
 
     def bytes(self) -> bytes:
         out = struct.pack("<III?", self.reg_pool, self.mem_pool, self.exg_pool, False)
-        out += u64(len(self.lut)) + bytes(self.lut) + vec([]) + vec([])
+        out += u64(len(self.lut)) + bytes(self.lut)
+        out += u64(len(self.reg_init)) + bytes(self.reg_init) + u64(len(self.mem_init)) + bytes(self.mem_init)
         out += u64(len(self.parts)) + b"".join(p.bytes() for p in self.parts)
         out += u64(len(self.regions))
         for r in self.regions:

@@ -1,0 +1,127 @@
+"""Design / symbol file format: byte compatibility with the reference
+serializer (src/Serializer.cpp) and initial state (src/SimInit.cpp)."""
+import ctypes as C
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from toucangpurt_gb300 import capi, sim, workloads
+
+REF_TOOL = pyoracle.REF_TOOL
+need_ref = pytest.mark.skipif(not REF_TOOL.exists(), reason="reference checkout not built here (oracle/_ref)")
+
+CFGS = {
+    "small": workloads.design_config("small"),
+    "vec_mem": dict(seed=12, n_lut=6000, levels=12, operands=3, palette_pct=40, ff_bits=2048, pi_bits=64,
+                    n_vec_ops=24, vec_nibbles=8, n_mems=3, mem_depth=512, mem_width=32, mem_read_ports=2,
+                    mem_write_ports=2, mem_multi_writer=1, luts_per_part=2500, cone_depth=2, with_stop=1),
+}
+
+
+@pytest.fixture(scope="module", params=list(CFGS))
+def design(request, tmp_path_factory, built):
+    d = tmp_path_factory.mktemp("fmt")
+    dp, sp = d / "d.bin", d / "s.bin"
+    info = sim.generate(dp, sp, **CFGS[request.param])
+    return dp, sp, info
+
+
+def _resave(fn, src, dst):
+    capi.check(fn(str(src).encode(), str(dst).encode()))
+
+
+def test_product_resave_is_byte_identical(design, tmp_path):
+    dp, sp, _ = design
+    _resave(capi.lib().tgs_resave_design, dp, tmp_path / "d2.bin")
+    assert (tmp_path / "d2.bin").read_bytes() == dp.read_bytes()
+    _resave(capi.lib().tgs_resave_symbols, sp, tmp_path / "s2.bin")
+    assert len((tmp_path / "s2.bin").read_bytes()) == len(sp.read_bytes())
+
+
+@need_ref
+def test_reference_serializer_roundtrip_byte_identical(design, tmp_path):
+    dp, sp, _ = design
+    out = tmp_path / "ref.bin"
+    subprocess.run([str(REF_TOOL), "roundtrip", str(dp), str(out)], check=True)
+    assert out.read_bytes() == dp.read_bytes()
+    r = subprocess.run([str(REF_TOOL), "identical", str(dp), str(out)], check=True, capture_output=True, text=True)
+    assert r.stdout.strip() == "identical"
+
+
+@need_ref
+def test_reference_reads_symbols(design, tmp_path):
+    dp, sp, _ = design
+    out = tmp_path / "sym.bin"
+    r = subprocess.run([str(REF_TOOL), "symtrip", str(sp), str(out)], check=True, capture_output=True, text=True)
+    n_regs, n_sig, n_mem = map(int, r.stdout.split())
+    assert n_regs > 0
+    # the product reads the reference's re-serialization (hash-map order may differ)
+    capi.check(capi.lib().tgs_resave_symbols(str(out).encode(), str(tmp_path / "again.bin").encode()))
+
+
+def _initial(dp, sp, randomize):
+    o = pyoracle.OracleDesign(dp, sp)
+    regs = np.zeros(o.reg_pool, np.uint8)
+    mems = np.zeros(o.mem_pool, np.uint8)
+    capi.check(capi.lib().tgs_initial_state(str(dp).encode(), str(sp).encode(), randomize,
+                                            regs.ctypes.data_as(capi.u8p), regs.size,
+                                            mems.ctypes.data_as(capi.u8p), mems.size))
+    return regs, mems
+
+
+@pytest.mark.parametrize("randomize", [0, 1])
+def test_initial_state_product_matches_oracle(design, randomize):
+    dp, sp, _ = design
+    regs, mems = _initial(dp, sp, randomize)
+    od = pyoracle.OracleDesign(dp, sp, randomize=bool(randomize))
+    np.testing.assert_array_equal(regs, od.initial_regs())
+    np.testing.assert_array_equal(mems, od.initial_mems())
+    if randomize:
+        assert regs.any()
+
+
+@need_ref
+def test_initial_state_matches_reference_randomize(design, tmp_path):
+    dp, sp, _ = design
+    r, m = tmp_path / "r.bin", tmp_path / "m.bin"
+    subprocess.run([str(REF_TOOL), "initstate", str(dp), str(sp), "1", str(r), str(m)], check=True)
+    regs, mems = _initial(dp, sp, 1)
+    np.testing.assert_array_equal(np.fromfile(r, np.uint8), regs)
+    np.testing.assert_array_equal(np.fromfile(m, np.uint8), mems)
+
+
+def test_truncated_and_corrupt_files(design, tmp_path):
+    dp, sp, _ = design
+    data = dp.read_bytes()
+    for cut in (3, 20, len(data) // 2, len(data) - 1):
+        p = tmp_path / f"cut{cut}.bin"
+        p.write_bytes(data[:cut])
+        with pytest.raises(capi.TgsError) as e:
+            sim.validate_file(p)
+        assert e.value.code == capi.ERR_FORMAT
+    # absurd vector count: rejected before any allocation
+    bad = bytearray(data)
+    bad[13:21] = (2**62).to_bytes(8, "little")  # lut vector count
+    p = tmp_path / "bad.bin"
+    p.write_bytes(bytes(bad))
+    with pytest.raises(capi.TgsError) as e:
+        sim.validate_file(p)
+    assert e.value.code == capi.ERR_FORMAT
+
+
+def test_missing_file(tmp_path):
+    with pytest.raises(capi.TgsError) as e:
+        sim.validate_file(tmp_path / "nope.bin")
+    assert e.value.code == capi.ERR_IO
+
+
+def test_oracle_parser_agrees_on_sizes(design):
+    dp, sp, info = design
+    od = pyoracle.OracleDesign(dp, sp)
+    assert od.reg_pool == info["reg_pool"]
+    assert od.mem_pool == info["mem_pool"]
+    assert od.lut_ops == info["lut_ops"]
+    assert od.lut_ops == sim.validate_file(dp, sp)

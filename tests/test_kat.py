@@ -349,3 +349,32 @@ def test_kat_stop_print_gpu(tmp_path, built, capfd):
     out = capfd.readouterr().out
     assert "stop-message" in out and "never" not in out
     assert "Toucan first stop" in out
+
+
+def kat_design_with_inputs(name: str) -> dl.Design:
+    """The case's design with its input registers (and memory) stored as the
+    initial regPool / memPool of the design file, for runs without a
+    testbench (the reference kernel in the golden fixtures)."""
+    if name == "mem_write":
+        d, regs, _ = case_mem_write()
+    elif name == "reg_copy_rounding":
+        d, regs, _ = case_reg_copy_rounding()
+        regs = np.zeros(16, np.uint8)
+        init = np.zeros(d.reg_pool, np.uint8)
+        init[16:24] = 5
+        init[24:32] = 7
+        d.reg_init = init.tobytes()
+        return d
+    elif name == "stop_print":
+        d = case_stop_print()
+        regs = np.zeros(16, np.uint8)
+        regs[1] = 4
+    else:
+        r = CASES[name]()
+        d, regs = r[0], r[1]
+        if len(r) > 3:
+            d.mem_init = np.asarray(r[3], np.uint8).tobytes()
+    init = np.zeros(d.reg_pool, np.uint8)
+    init[:16] = regs
+    d.reg_init = init.tobytes()
+    return d

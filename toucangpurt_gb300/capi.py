@@ -134,6 +134,9 @@ SIGNATURES = {
     "tgs_generate": [C.POINTER(GenConfig), C.c_char_p, C.c_char_p, C.POINTER(GenInfo)],
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
+    "tgs_resave_design": [C.c_char_p, C.c_char_p],
+    "tgs_resave_symbols": [C.c_char_p, C.c_char_p],
+    "tgs_initial_state": [C.c_char_p, C.c_char_p, C.c_int, u8p, C.c_size_t, u8p, C.c_size_t],
 }
 
 

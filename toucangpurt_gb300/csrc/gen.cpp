@@ -48,6 +48,32 @@ using namespace toucanGPUSim;
 constexpr uint16_t kMux = 1, kAdd = 520, kSub = 776, kAnd = 1032, kOr = 1288, kXor = 1544, kEq = 1800, kUlt = 2056;
 constexpr uint16_t kForceBase = 2600;  // 16-entry windows: (c & ~(P-1)) | p
 
+// Records are written to the file as raw bytes, padding included.  A copy
+// of a struct may skip its padding, so every padded record is zeroed in
+// place inside its vector before its fields are set: files are reproducible.
+template <typename T>
+T &addZeroed(std::vector<T> &v) {
+  v.emplace_back();
+  T &t = v.back();
+  std::memset(static_cast<void *>(&t), 0, sizeof(T));
+  return t;
+}
+void addRegRead(std::vector<CGRegReadMetaInfo> &v, uint32_t reg, uint16_t slot) {
+  auto &r = addZeroed(v);
+  r.reg = reg;
+  r.result = slot;
+}
+void addExgRead(std::vector<CGExchangeReadMetaInfo> &v, uint32_t e, uint16_t slot) {
+  auto &r = addZeroed(v);
+  r.exchange = e;
+  r.result = slot;
+}
+void addWriteBack(std::vector<CGMicroPartLUTLastLevelWriteBack> &v, uint8_t src, uint16_t slot) {
+  auto &r = addZeroed(v);
+  r.shuffleId = src;
+  r.result = slot;
+}
+
 struct Rng {
   uint64_t s;
   explicit Rng(uint64_t seed) : s(mix64(seed ^ 0x5EEDull)) {}
@@ -141,9 +167,9 @@ class PartGen {
   uint16_t addInput(uint32_t src, bool exchange) {
     uint16_t s = slot(1);
     if (exchange)
-      P_.ops_l0_exchangeRead.push_back({src, s});
+      addExgRead(P_.ops_l0_exchangeRead, src, s);
     else
-      P_.ops_l0_regRead.push_back({src, s});
+      addRegRead(P_.ops_l0_regRead, src, s);
     ++cnt_.l0;
     inputs_.vals.push_back({s, false});
     return s;
@@ -192,7 +218,7 @@ class PartGen {
         for (uint32_t l = 0; l < lanes; ++l) {
           uint32_t idx = made + l;
           uint16_t dst = (last && idx < nOut) ? uint16_t(outBase + idx) : uint16_t(ring[b % (R + 2)] + (idx % ringBlock));
-          m.lastLevel.push_back({uint8_t(32 + l), dst});
+          addWriteBack(m.lastLevel, uint8_t(32 + l), dst);
           band.vals.push_back({dst, bit[l]});
         }
         made += lanes;
@@ -232,7 +258,7 @@ class PartGen {
         }
       }
       m.topLevel.push_back(op);
-      m.lastLevel.push_back({uint8_t(32 + j), uint16_t(base + j)});
+      addWriteBack(m.lastLevel, uint8_t(32 + j), uint16_t(base + j));
     }
     level.push_back(std::move(m));
     ++cnt_.mparts;
@@ -519,7 +545,7 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
         CGMicroPartInfo m;
         m.isLUTPart = false;
         for (size_t v = v0; v < std::min(vecGroups.size(), v0 + 32); ++v) {
-          CGMicroPartVecArithOrLogic op{};
+          auto &op = addZeroed(m.vecArithAndLogic);
           op.vec1Base = vecGroups[v].first;
           op.vec2Base = vecGroups[v].second;
           op.vecLength = uint16_t(vn);
@@ -532,7 +558,6 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
             for (uint32_t j = 0; j < vn; ++j) vecResults.push_back(uint16_t(op.result + j));
           else
             vecResults.push_back(op.result);
-          m.vecArithAndLogic.push_back(op);
           ++cnt.vec;
         }
         lvl.push_back(std::move(m));
@@ -558,14 +583,13 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
           CGMicroPartInfo m;
           m.isLUTPart = false;
           for (uint32_t j = j0; j < std::min(mp.nibbles, j0 + 32); ++j) {
-            CGMicroPartMemRead op{};
+            auto &op = addZeroed(m.memRead);
             op.hasMultipleWriter = mp.multi;
             op.memBase = mp.nibBase[j];
             op.en = 1;
             op.addrVec = addr;
             op.result = g.slot(1);
             produced.push_back(op.result);
-            m.memRead.push_back(op);
             ++cnt.memR;
           }
           readLvl.push_back(std::move(m));
@@ -577,7 +601,7 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
         CGMicroPartInfo m;
         m.isLUTPart = false;
         for (size_t v = 0; v < vecGroups.size() && v < 32; ++v) {
-          CGMicroPartVecRead op{};
+          auto &op = addZeroed(m.vecRead);
           op.vecBase = vecGroups[v].first;
           op.vecLength = uint16_t(vn);
           op.offset = uint16_t(rng.below(4));
@@ -587,7 +611,6 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
           op.outRangeValue = 0;
           op.result = g.slot(1);
           produced.push_back(op.result);
-          m.vecRead.push_back(op);
         }
         vrLvl.push_back(std::move(m));
         ++cnt.mparts;
@@ -633,13 +656,12 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
         const MemPlan &mp = mems[mw.first];
         uint16_t addr = g.addressGen(mp.addrBits, writePorts, mw.second, addrLvl);
         for (uint32_t j = 0; j < mp.nibbles; ++j) {
-          CGMemWriteMetaInfo op{};
+          auto &op = addZeroed(part.ops_last_memWrite);
           op.hasMultipleWriter = mp.multi;
           op.memBase = mp.nibBase[j];
           op.addrVec = addr;
           op.dat = g.anyRecent();
           op.en = 1;
-          part.ops_last_memWrite.push_back(op);
           ++cnt.memW;
         }
       }

@@ -911,3 +911,48 @@ extern "C" int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *o) {
     o->makespan[1] = h->sched.makespan[1];
   });
 }
+
+extern "C" int tgs_resave_design(const char *in, const char *out) {
+  return guard([&] {
+    if (!in || !out) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(in);
+    SimDesignInfo d;
+    parseDesign(bytes.data(), bytes.size(), d);
+    std::ofstream o(out, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
+    serializeSimDesignInfo(o, d);
+  });
+}
+
+extern "C" int tgs_resave_symbols(const char *in, const char *out) {
+  return guard([&] {
+    if (!in || !out) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(in);
+    SimDebugInfo s;
+    parseSymbols(bytes.data(), bytes.size(), s);
+    std::ofstream o(out, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
+    serializeSimDebugInfo(o, s);
+  });
+}
+
+extern "C" int tgs_initial_state(const char *design_path, const char *symbol_path, int randomize, uint8_t *regs,
+                                 size_t reg_bytes, uint8_t *mems, size_t mem_bytes) {
+  return guard([&] {
+    if (!design_path) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(design_path);
+    SimDesignInfo d;
+    SimDebugInfo s;
+    parseDesign(bytes.data(), bytes.size(), d);
+    if (symbol_path) {
+      auto sb = readFileBytes(symbol_path);
+      parseSymbols(sb.data(), sb.size(), s);
+    }
+    d.Init();
+    if (randomize) d.Randomize(0, s);
+    if (reg_bytes != d.regPool.size() || mem_bytes != d.memPool.size())
+      throw Error(TGS_ERR_ARG, "buffers must hold regPoolSize and memPoolSize bytes");
+    if (regs && reg_bytes) std::memcpy(regs, d.regPool.data(), reg_bytes);
+    if (mems && mem_bytes) std::memcpy(mems, d.memPool.data(), mem_bytes);
+  });
+}
