@@ -163,4 +163,6 @@ class OracleState:
         return np.ctypeslib.as_array(lib().orc_state_regs(self._s), (self.d.reg_pool,))
 
     def mems(self) -> np.ndarray:
-        return np.ctypeslib.as_array(lib().orc_state_mems(self._s), (max(1, self.d.mem_pool),))[: self.d.mem_pool]
+        if self.d.mem_pool == 0:
+            return np.zeros(0, np.uint8)
+        return np.ctypeslib.as_array(lib().orc_state_mems(self._s), (self.d.mem_pool,))
