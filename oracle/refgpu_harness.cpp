@@ -338,6 +338,10 @@ int main(int argc, char **argv) {
       uint64_t roll = 0;
       uint32_t stopCycle = 0xFFFFFFFFu;
       std::ostringstream cyc;
+      CUevent ev0, ev1;
+      CK(cuEventCreate(&ev0, CU_EVENT_DEFAULT));
+      CK(cuEventCreate(&ev1, CU_EVENT_DEFAULT));
+      float kernelMs = 0.0f;
       if (mode == "eval") {
         for (uint32_t c = 0; c < cycles; ++c) {
           CK(cuMemcpyDtoH(regs.data(), regDev, regs.size()));
@@ -347,8 +351,13 @@ int main(int argc, char **argv) {
           roll = mix64(roll + dg);
           cyc << (c ? "," : "") << hex(dg);
           void *args[] = {nullptr};
+          CK(cuEventRecord(ev0, nullptr));
           CK(cuLaunchCooperativeKernel(M.single, gridSingle, 1, 1, threads, 1, 1, unsigned(maxVp), nullptr, args));
+          CK(cuEventRecord(ev1, nullptr));
           CK(cuCtxSynchronize());
+          float ms = 0;
+          CK(cuEventElapsedTime(&ms, ev0, ev1));
+          kernelMs += ms;
           uint32_t stop = 0;
           CK(cuMemcpyDtoH(&stop, stopDev, 4));
           if (stop && stopCycle == 0xFFFFFFFFu) stopCycle = c;
@@ -357,17 +366,23 @@ int main(int argc, char **argv) {
         uint32_t n = cycles;
         void *args[] = {&n};
         CUfunction f = maxParts > gridMulti ? M.freeLarge : M.freeRun;
+        CK(cuEventRecord(ev0, nullptr));
         CK(cuLaunchCooperativeKernel(f, gridMulti, 1, 1, threads, 1, 1, unsigned(maxVp), nullptr, args));
+        CK(cuEventRecord(ev1, nullptr));
         CK(cuCtxSynchronize());
+        CK(cuEventElapsedTime(&kernelMs, ev0, ev1));
       }
       CK(cuMemcpyDtoH(regs.data(), regDev, regs.size()));
       if (!mems.empty()) CK(cuMemcpyDtoH(mems.data(), memDev, mems.size()));
+      cuEventDestroy(ev0);
+      cuEventDestroy(ev1);
       uint32_t real = 0, stop = 0;
       CK(cuMemcpyDtoH(&real, realDev, 4));
       CK(cuMemcpyDtoH(&stop, stopDev, 4));
       out << "{\"stream\": " << s << ", \"mode\": \"" << mode << "\", \"cycles\": " << cycles
           << ", \"final_reg_digest\": " << hex(digest(regs)) << ", \"final_mem_digest\": " << hex(digest(mems))
           << ", \"rolling_digest\": " << hex(roll) << ", \"stop\": " << stop << ", \"stop_cycle\": " << stopCycle
+          << ", \"kernel_ms\": " << kernelMs << ", \"large_kernel\": " << (maxParts > gridMulti ? 1 : 0)
           << ", \"real_cycles\": " << real << ", \"threads\": " << threads << ", \"grid_single\": " << gridSingle
           << ", \"grid_multi\": " << gridMulti << ", \"cycle_digests\": [" << cyc.str() << "]";
       auto dump = [&](const char *key, const std::vector<uint8_t> &v) {
