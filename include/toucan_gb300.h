@@ -137,6 +137,21 @@ int tgs_state_digest(tgs_sim *h, uint32_t stream, uint64_t *reg_digest, uint64_t
 /* Reset every stream to the initial state (Init/Randomize result). */
 int tgs_reset_state(tgs_sim *h);
 
+/* Same digest as tgs_state_digest, of caller-owned device memory, for
+ * callers that cannot allocate device memory (an allocator that owns every
+ * device byte, a frozen memory pool).  No counterpart in the reference.
+ * pools: device pointer, pool i at pools + i * stride, `bytes` bytes each
+ * (bytes < 4 GiB); digests: host array of n_pools results.  At most 4,096
+ * pools per call (TGS_ERR_RANGE above that).  Allocates nothing: the
+ * per-pool accumulators are a fixed 32 KiB device array inside the library,
+ * present on every GPU that loads it until the process exits.  The first
+ * call on a device resolves that array's device address (with the device
+ * current), so make it before any stream capture.  Runs on the legacy
+ * default stream and waits for it; all calls share the one array, so calls
+ * that overlap on the GPU (other host threads) race. */
+int tgs_pool_digests_noalloc(const uint8_t *pools, uint64_t stride, uint64_t bytes, uint32_t n_pools,
+                             uint64_t *digests);
+
 /* ---- batched stimulus runs (new) -------------------------------------- */
 /* Stimulus: the listed register nibbles are rewritten before every cycle.
  *   seed_s = mix64(base_seed ^ s); h = mix64(seed_s ^ mix64((c << 32) | i))

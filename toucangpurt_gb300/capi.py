@@ -128,6 +128,7 @@ SIGNATURES = {
     "tgs_write_mem_pool": [C.c_void_p, C.c_uint32, u8p, C.c_size_t],
     "tgs_state_digest": [C.c_void_p, C.c_uint32, u64p, u64p],
     "tgs_reset_state": [C.c_void_p],
+    "tgs_pool_digests_noalloc": [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint32, u64p],
     "tgs_batch_run": [C.c_void_p, C.POINTER(Batch), C.POINTER(BatchResult)],
     "tgs_get_design_stats": [C.c_void_p, C.POINTER(DesignStats)],
     "tgs_default_gen_config": [C.POINTER(GenConfig)],
