@@ -40,7 +40,7 @@ def args_parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-gpu"])
     p.add_argument("--workload", default="largest")
     p.add_argument("--cycles-per-step", type=int, default=0)
     p.add_argument("--streams", type=int, default=0)
@@ -219,6 +219,42 @@ def run_reference(a, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_gpu(a, rank, ws):
+    """The reference's own GPU kernel (src/SimEval.cu built unmodified into
+    oracle/_ref/ref_simeval.cubin, driven by oracle/refgpu_harness.cpp) on the
+    same design: one stream (the reference cannot batch), free running
+    (eval_free_running) and one cooperative launch per cycle with host-side
+    stimulus (eval() + setRegister)."""
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    from toucangpurt_gb300 import build
+
+    build.build()
+    pyoracle.build()
+    exe, cubin = pyoracle.HERE / "_build" / "refgpu", pyoracle.REF_CUBIN
+    if not exe.exists() or not cubin.exists():
+        print(json.dumps({"impl": "reference-gpu", "unavailable": "reference cubin not built (needs the reference checkout)"}))
+        return
+    wd = Path(tempfile.mkdtemp(prefix="tgs_refgpu_"))
+    dp, sp, info = make_design(a.workload, wd, 0, a.override)
+    stim = wd / "stim.txt"
+    stim.write_text(f"1234 {len(info['pi_ids'])}\n" + "".join(f"{int(r)} {int(b)} 0\n" for r, b in zip(info["pi_ids"], info["pi_bits"])))
+    res = {}
+    for mode, cycles in (("free", a.cycles_per_step or 20), ("eval", max(1, (a.cycles_per_step or 20) // 4))):
+        out = wd / f"{mode}.jsonl"
+        subprocess.run([str(exe), str(cubin), str(dp), str(sp), "0", mode, str(cycles), "1",
+                        str(stim) if mode == "eval" else "-", str(out)], check=True, timeout=1800)
+        r = json.loads(out.read_text().splitlines()[0])
+        res[mode] = {"cycles": cycles, "kernel_ms": r["kernel_ms"], "stimulus_cycles_per_s": cycles / (r["kernel_ms"] / 1e3),
+                     "large_kernel": r["large_kernel"], "grid": r["grid_multi"] if mode == "free" else r["grid_single"],
+                     "threads": r["threads"]}
+    line = {"impl": "reference-gpu", "metric": METRIC, "unit": "stimulus-cycles/s",
+            "value": res["free"]["stimulus_cycles_per_s"], "lut_evals_per_s": res["free"]["stimulus_cycles_per_s"] * info["lut_ops"],
+            "config": {"workload": f"{a.workload}: {info['lut_ops']} LUT ops, 1 stream"}, "modes": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_gb300(a, rank, ws):
     from toucangpurt_gb300 import build, sim, workloads
 
@@ -293,6 +329,8 @@ def main():
     rank, ws = dist_init()
     if a.impl == "reference":
         run_reference(a, rank, ws)
+    elif a.impl == "reference-gpu":
+        run_reference_gpu(a, rank, ws)
     else:
         run_gb300(a, rank, ws)
 

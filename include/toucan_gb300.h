@@ -66,7 +66,7 @@ typedef struct tgs_options {
   uint32_t mode;             /* TGS_MODE_PERSISTENT or TGS_MODE_GRAPH */
   uint32_t barrier_timeout_ms; /* budget of every device-side wait (default 2000) */
   uint32_t validate;         /* 1 = run the static design checks at init (default 1) */
-  uint32_t resident_netlist; /* 1 = keep each block's netlist in shared memory when it fits */
+  uint32_t resident_netlist; /* 0: stage each exec level into shared memory when it fits (default); 2: read levels from global memory */
   uint32_t reserved[7];
 } tgs_options;
 

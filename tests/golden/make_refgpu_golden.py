@@ -22,7 +22,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-# name -> generator fields (uniform fan-out keeps generation free of floating point)
+# name -> generator fields
 GEN_CASES = {
     "small": dict(seed=101, n_lut=4096, levels=16, operands=2, ff_bits=512, pi_bits=32, n_mems=1, mem_depth=1024,
                   mem_width=32, mem_read_ports=1, mem_write_ports=1, luts_per_part=2048),

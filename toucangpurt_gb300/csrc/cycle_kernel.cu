@@ -135,7 +135,7 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
   uint32_t v[G];
   // top level: operands < 16 are immediates, else value-pool slots
   if (lane < W) {
-    const uint2 t = __ldg(reinterpret_cast<const uint2 *>(top) + lane);
+    const uint2 t = reinterpret_cast<const uint2 *>(top)[lane];
     const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
     uint32_t A[G], B[G], C[G];
     if (a < 16) {
@@ -165,7 +165,7 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
   // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
   const uint32_t *mid = top + 2 * W;
   for (uint32_t m = 0; m < nMid; ++m) {
-    const uint32_t w = lane < W ? __ldg(mid + m * W + lane) : 0u;
+    const uint32_t w = lane < W ? mid[m * W + lane] : 0u;
     const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
     uint32_t nv[G];
 #pragma unroll
@@ -183,7 +183,7 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
   }
   // write-back: shuffleId < 32 immediate, else lane (shuffleId mod 32)
   const uint32_t *wb = mid + nMid * W;
-  const uint32_t wv = lane < nWB ? __ldg(wb + lane) : 0u;
+  const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;
   uint32_t out[G];
 #pragma unroll
@@ -203,7 +203,7 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
   const uint32_t *r = mp + kMPHeaderWords + lane * kVecReadWords;
-  const uint32_t w0 = __ldg(r), w1 = __ldg(r + 1), w2 = __ldg(r + 2), w3 = __ldg(r + 3), w4 = __ldg(r + 4);
+  const uint32_t w0 = r[0], w1 = r[1], w2 = r[2], w3 = r[3], w4 = r[4];
   const uint32_t base = w0 & 0xFFFFu, len = w0 >> 16, off = w1 & 0xFFFFu, isConst = (w1 >> 16) & 1u;
   const uint32_t ix[4] = {w2 & 0xFFFFu, w2 >> 16, w3 & 0xFFFFu, w3 >> 16};
   const uint32_t outR = w4 & 0xFFFFu, res = w4 >> 16;
@@ -237,7 +237,7 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *_
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
   const uint32_t *r = mp + kMPHeaderWords + lane * kVecOpWords;
-  const uint32_t w0 = __ldg(r), w1 = __ldg(r + 1), res = __ldg(r + 2);
+  const uint32_t w0 = r[0], w1 = r[1], res = r[2];
   const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = w1 & 0xFFFFu, op = (w1 >> 16) & 0xFFu, cf = w1 >> 24;
   const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
   const uint8_t *cv = p.constVec + d.constOff;
@@ -288,7 +288,7 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
   const uint32_t *r = mp + kMPHeaderWords + lane * kMemReadWords;
-  const uint32_t lo = __ldg(r), hi = __ldg(r + 1), w2 = __ldg(r + 2), res = __ldg(r + 3);
+  const uint32_t lo = r[0], hi = r[1], w2 = r[2], res = r[3];
   const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
   const bool multi = (hi >> 31) != 0;
   const uint32_t en = w2 & 0xFFFFu, av = w2 >> 16;
@@ -319,13 +319,62 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
   }
 }
 
+// ---- exec-level staging ------------------------------------------------------
+// Two shared-memory buffers, one mbarrier each.  Thread 0 issues the bulk copy
+// of level lv + 1 right after the block barrier that opens level lv (so every
+// thread is done with the buffer's previous level); every thread waits on the
+// buffer's phase parity before reading it.  Waits are bounded.
+struct Stage {
+  uint32_t *buf[2];
+  uint32_t mb[2];     // shared-memory addresses of the mbarriers
+  uint32_t uses[2];   // completed uses per buffer (phase parity)
+};
+
+__device__ __forceinline__ void stageIssue(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words) {
+  const uint32_t bytes = words * 4u;
+  const uint32_t dst = uint32_t(__cvta_generic_to_shared(st.buf[b]));
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(st.mb[b]), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(st.mb[b])
+               : "memory");
+}
+
+__device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t b) {
+  const uint32_t parity = st.uses[b] & 1u;
+  uint32_t done = 0;
+  unsigned long long t0 = 0;
+  for (uint32_t spin = 0; !done; ++spin) {
+    asm volatile(
+        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\tselp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(done)
+        : "r"(st.mb[b]), "r"(parity)
+        : "memory");
+    if (!done) {
+      if (spin == 0) t0 = gtimer();
+      else if (gtimer() - t0 > p.timeoutNs) {
+        raiseErr(p, kErrTimeout, blockIdx.x, 0xFFFFFFFEu, b);
+        return false;
+      }
+    }
+  }
+  st.uses[b]++;
+  return true;
+}
+
 // ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
 template <int SPW, int G>
 __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__ vp, const uint8_t *__restrict__ tab,
-                         uint32_t cycle) {
+                         Stage &st, uint32_t cycle) {
   const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
   const PartDesc &d = p.parts[pid];
   const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
+  const uint2 *ld = p.levelDesc + d.schedOff;
+  const uint32_t cap = p.stageWords;
+  // the first exec level streams in while the level-0 reads run
+  if (cap && tid == 0 && d.nLevels) {
+    const uint2 l0 = ld[0];
+    if (l0.y <= cap) stageIssue(st, 0, p.sched + l0.x, l0.y);
+  }
 
   // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
   {
@@ -342,15 +391,27 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
   __syncthreads();
 
   // exec levels: warp w runs the micro-partitions the schedule gave it
-  const uint32_t *sc = p.sched + d.schedOff;
   for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
-    const uint32_t flags = __ldg(sc);
-    if (lv > 0 && (flags & 1u)) __syncthreads();
-    const uint32_t ub = __ldg(sc + 1 + warp), ue = __ldg(sc + 2 + warp);
-    const uint32_t *units = sc + 2 + NW;
+    const uint2 cur = ld[lv];
+    const uint32_t *blk = p.sched + cur.x;
+    if (cap) {
+      if (lv > 0) __syncthreads();  // staged buffers are reused every second level
+      if (tid == 0 && lv + 1 < d.nLevels) {
+        const uint2 nx = ld[lv + 1];
+        if (nx.y <= cap) stageIssue(st, (lv + 1) & 1u, p.sched + nx.x, nx.y);
+      }
+      // on a (never expected) wait timeout the level is read from global
+      // memory instead: same words, uniform control flow, and the error word
+      // ends the launch at the next grid barrier
+      if (cur.y <= cap && stageWait(p, st, lv & 1u)) blk = st.buf[lv & 1u];
+    } else if (lv > 0 && (blk[0] & 1u)) {
+      __syncthreads();
+    }
+    const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
+    const uint32_t *units = blk + 2 + NW;
     for (uint32_t u = ub; u < ue; ++u) {
-      const uint32_t *mp = p.net + __ldg(units + u);
-      const uint32_t hdr = __ldg(mp);
+      const uint32_t *mp = blk + units[u];
+      const uint32_t hdr = mp[0];
       switch (hdr & 3u) {
         case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;
         case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane); break;
@@ -359,7 +420,6 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
       }
       __syncwarp();
     }
-    sc = units + __ldg(sc + 1 + NW);
   }
   __syncthreads();
 
@@ -572,8 +632,19 @@ __device__ bool stageTable(const KParams &p, uint8_t *tab) {
 template <int SPW, int G>
 __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0, uint32_t nCycles) {
   extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) unsigned long long stageMbar[2];
   uint8_t *tab = smem;
-  uint32_t *vp = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
+  Stage st;
+  st.buf[0] = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
+  st.buf[1] = st.buf[0] + p.stageWords;
+  st.mb[0] = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
+  st.mb[1] = uint32_t(__cvta_generic_to_shared(&stageMbar[1]));
+  st.uses[0] = st.uses[1] = 0;
+  uint32_t *vp = st.buf[1] + p.stageWords;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st.mb[0]) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st.mb[1]) : "memory");
+  }
   const bool staged = stageTable(p, tab);
   __syncthreads();
   if (!staged) return;
@@ -592,7 +663,7 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
       for (uint32_t i = b; i < e; ++i) {
         const long long t0 = clock64();
         const uint32_t item = __ldg(p.items + i);
-        evalItem<SPW, G>(p, item, vp, tab, t);
+        evalItem<SPW, G>(p, item, vp, tab, st, t);
         // per-partition clock64 profile (SimEval.cu:894-983): running mean of
         // the useful ticks over cycles [100, 200) of group block 0
         if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {

@@ -12,6 +12,8 @@
 // word holding the nibbles of 8 streams (stream k of a group in bits
 // 4k..4k+3).  The reference stores one stream, one nibble per byte.
 #pragma once
+#include <vector_types.h>
+
 #include <cstdint>
 
 namespace tgs {
@@ -52,16 +54,21 @@ struct PartDesc {
 };
 static_assert(sizeof(PartDesc) == 96, "PartDesc size");
 
-// Warp schedule of a partition (at PartDesc::schedOff), for NW warps:
-//   per exec level: 1 word flags (bit0: block barrier before the level),
-//                   NW + 1 words: prefix offsets into the unit list of the level,
-//                   then the unit list: word offsets of micro-partitions.
-// Levels are stored back to back; level k's record starts where k-1's ends.
+// Exec levels (KParams::sched), for NW warps: one 16-byte aligned block per
+// partition level, [flags (bit0: block barrier)][NW + 1 prefix offsets into
+// the unit list][unit list: word offsets of the micro-partitions relative to
+// the block][micro-partition records in warp order].  KParams::levelDesc
+// holds (block offset, block words) per level; PartDesc::schedOff indexes
+// the partition's first level there.  A block is staged into shared memory
+// with one bulk async copy while the previous level computes.
 
 // Kernel parameters (passed by value).
 struct KParams {
   const uint32_t *net;        // design words
-  const uint32_t *sched;      // warp schedules (PartDesc::schedOff)
+  const uint32_t *sched;      // exec-level blocks
+  const uint2 *levelDesc;     // (block offset, words) per partition level
+  uint32_t stageWords;        // capacity of each shared-memory stage buffer (0 = no staging)
+  uint32_t stagePad;
   const PartDesc *parts;
   const uint8_t *constVec;
   const uint8_t *lutTable;    // 4642 entries, padded to 4656

@@ -205,6 +205,7 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img) {
         MPartRef ref;
         ref.feat.partLevels = pd.nLevels;
         ref.off = m.isLUTPart ? emitLut(m, net, ref.feat) : emitSpecial(m, net, ref.feat);
+        ref.words = uint32_t((net.size() + 3) / 4 * 4) - ref.off;
         accessOf(m, ref.reads, ref.writes);
         std::sort(ref.reads.begin(), ref.reads.end());
         ref.reads.erase(std::unique(ref.reads.begin(), ref.reads.end()), ref.reads.end());
@@ -264,7 +265,7 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
   auto &sw = out.words;
   for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
     PartDesc &pd = img.parts[pid];
-    pd.schedOff = uint32_t(sw.size());
+    pd.schedOff = uint32_t(out.levelDesc.size() / 2);
     double total = 0;
     // barrier placement: hazards since the last block barrier, tracked per slot
     std::vector<int32_t> lastWriter(pd.vpSlots + 64, -1);  // warp of last write since the barrier
@@ -309,6 +310,11 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
           for (uint32_t s : mps[i].writes) { lastWriter[s] = int32_t(w); touched.push_back(s); }
         }
       out.levels++;
+      // level block: [flags][NW + 1 prefix offsets][unit offsets][pad][micro-partitions in warp order]
+      while (sw.size() % 4) sw.push_back(0);
+      const uint32_t blk = uint32_t(sw.size());
+      uint32_t nUnits = 0;
+      for (uint32_t w = 0; w < NW; ++w) nUnits += uint32_t(perWarp[w].size());
       sw.push_back(need ? 1u : 0u);
       uint32_t acc = 0;
       for (uint32_t w = 0; w < NW; ++w) {
@@ -316,14 +322,28 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
         acc += uint32_t(perWarp[w].size());
       }
       sw.push_back(acc);
+      const uint32_t unitBase = uint32_t(sw.size());
+      sw.resize(sw.size() + nUnits, 0);
+      while (sw.size() % 4) sw.push_back(0);
+      uint32_t u = 0;
       for (uint32_t w = 0; w < NW; ++w)
-        for (uint32_t i : perWarp[w]) sw.push_back(mps[i].off);
+        for (uint32_t i : perWarp[w]) {
+          sw[unitBase + u++] = uint32_t(sw.size()) - blk;
+          const MPartRef &r = mps[i];
+          sw.insert(sw.end(), img.net.begin() + r.off, img.net.begin() + r.off + r.words);
+          while (sw.size() % 4) sw.push_back(0);
+        }
+      const uint32_t words = uint32_t(sw.size()) - blk;
+      out.levelDesc.push_back(blk);
+      out.levelDesc.push_back(words);
+      out.maxLevelWords = std::max(out.maxLevelWords, words);
     }
     // L0 and last level scale with their op counts spread over the block
     total += double(pd.l0Count + pd.copySlots + 8 * pd.memWCount) / double(32 * NW) + 1.0;
     out.partCost[pid] = total;
   }
-  if (sw.empty()) sw.push_back(0);
+  while (sw.size() % 4 || sw.empty()) sw.push_back(0);
+  if (out.levelDesc.empty()) out.levelDesc.assign(2, 0);
 
   // items (partition, group block) onto blocks, per region, LPT by cost
   out.items.clear();

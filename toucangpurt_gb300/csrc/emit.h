@@ -27,7 +27,8 @@ struct MPartFeat {
 };
 
 struct MPartRef {
-  uint32_t off = 0;  // word offset in DeviceImage::net
+  uint32_t off = 0;    // word offset in DeviceImage::net
+  uint32_t words = 0;  // record size, multiple of 4
   MPartFeat feat;
   std::vector<uint32_t> reads, writes;
 };
@@ -43,7 +44,13 @@ struct DeviceImage {
 
 struct Schedule {
   uint32_t NW = 0;
-  std::vector<uint32_t> words;      // per-partition warp schedules (PartDesc::schedOff)
+  // exec-level blocks: per partition and level, [flags][NW + 1 prefix
+  // offsets][unit offsets][micro-partition records in warp order], 16-byte
+  // aligned so a level is one bulk copy; levelDesc = (block offset, words)
+  // per level, PartDesc::schedOff indexes the partition's first level
+  std::vector<uint32_t> words;
+  std::vector<uint32_t> levelDesc;
+  uint32_t maxLevelWords = 0;
   std::vector<uint32_t> items;      // (part | groupBlock << 20) per region and block
   std::vector<uint32_t> itemBegin;  // [2][nBlocks + 1]
   std::vector<double> partCost;

@@ -79,7 +79,6 @@ struct Rng {
   explicit Rng(uint64_t seed) : s(mix64(seed ^ 0x5EEDull)) {}
   uint64_t next() { return mix64(s += 0x9E3779B97F4A7C15ull); }
   uint32_t below(uint32_t n) { return n ? uint32_t((next() >> 32) * n >> 32) : 0; }
-  double real() { return double(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
 uint16_t forceWindow(uint32_t ports, uint32_t p) {
@@ -146,7 +145,7 @@ struct Val {
 
 struct Band {
   std::vector<Val> vals;
-  std::vector<double> cum;  // prefix sums of popularity weights
+  std::vector<uint64_t> cum;  // prefix sums of popularity weights
 };
 
 struct PartKind {
@@ -282,15 +281,40 @@ class PartGen {
   Counts &counts() { return cnt_; }
 
  private:
+  // Popularity weights follow a discrete power law: weight 2^k with
+  // P(k) proportional to 2^(-k (alpha - 1)), k = 0 .. log2(maxFan), so that
+  // P(weight >= x) ~ x^-(alpha - 1).  Only integers after one rounding of the
+  // class ratio to 32-bit fixed point: designs are identical on every host.
   void weigh(Band &b) {
     b.cum.resize(b.vals.size());
-    double acc = 0;
+    uint64_t acc = 0;
     for (size_t i = 0; i < b.vals.size(); ++i) {
-      double w = 1.0;
-      if (k_.alpha > 1.0) w = std::min(std::pow(1.0 - rng_.real(), -1.0 / (k_.alpha - 1.0)), double(k_.maxFan));
-      acc += w;
+      acc += k_.alpha > 1.0 ? (uint64_t(1) << weightClass()) : 1u;
       b.cum[i] = acc;
     }
+  }
+
+  uint32_t weightClass() {
+    if (classThr_.empty()) {
+      uint32_t kmax = 0;
+      while ((2u << kmax) <= std::max<uint32_t>(1, k_.maxFan)) ++kmax;
+      const uint64_t ratio = uint64_t(std::llround(std::exp2(-(k_.alpha - 1.0)) * 4294967296.0));  // Q32
+      std::vector<uint64_t> p(kmax + 1);
+      p[0] = uint64_t(1) << 32;
+      for (uint32_t k = 1; k <= kmax; ++k) p[k] = (p[k - 1] * ratio) >> 32;
+      uint64_t total = 0;
+      for (auto v : p) total += v;
+      uint64_t run = 0;
+      for (uint32_t k = 0; k <= kmax; ++k) {
+        run += p[k];
+        classThr_.push_back(uint64_t((unsigned __int128)run * 0xFFFFFFFFull / total));
+      }
+      classThr_.back() = 0xFFFFFFFFull;
+    }
+    const uint64_t u = rng_.next() >> 32;
+    uint32_t k = 0;
+    while (k + 1 < classThr_.size() && u > classThr_[k]) ++k;
+    return k;
   }
 
   // Operand for band b: uniformly one of the previous 1-3 bands (inputs
@@ -307,7 +331,7 @@ class PartGen {
         if (v.bit) return v;
       }
     }
-    double r = rng_.real() * src->cum.back();
+    const uint64_t r = 1 + uint64_t((unsigned __int128)(rng_.next()) * src->cum.back() >> 64);
     size_t i = std::lower_bound(src->cum.begin(), src->cum.end(), r) - src->cum.begin();
     return src->vals[std::min(i, src->vals.size() - 1)];
   }
@@ -378,6 +402,7 @@ class PartGen {
   uint32_t next_ = 16;
   Band inputs_;
   std::vector<Band> bands_;
+  std::vector<uint64_t> classThr_;
 };
 
 struct MemPlan {

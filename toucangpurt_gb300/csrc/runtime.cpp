@@ -88,11 +88,11 @@ struct tgs_sim {
 
   // launch configuration
   tgs::LaunchCfg lc;
-  uint32_t spw = 1, groups = 1, gpad = 1, nStreams = 1, regSlots = 4, exgSlots = 4;
+  uint32_t spw = 1, groups = 1, gpad = 1, nStreams = 1, regSlots = 4, exgSlots = 4, stageWords = 0;
   unsigned long long memStride = 16;
 
   // device memory
-  tgs::DBuf<uint32_t> net, schedW, items, itemBegin, regs, exg, stop, stopCycle, err, errInfo, barrier, realCycles, stimReg;
+  tgs::DBuf<uint32_t> net, schedW, levelDesc, items, itemBegin, regs, exg, stop, stopCycle, err, errInfo, barrier, realCycles, stimReg;
   tgs::DBuf<tgs::PartDesc> parts;
   tgs::DBuf<uint8_t> constVec, lutTable, mems, initRegs, initMems, stimBits;
   tgs::DBuf<uint16_t> stimToggle;
@@ -144,6 +144,8 @@ void fillParams(tgs_sim *h) {
   std::memset(&p, 0, sizeof(p));
   p.net = h->net.p;
   p.sched = h->schedW.p;
+  p.levelDesc = reinterpret_cast<const uint2 *>(h->levelDesc.p);
+  p.stageWords = h->stageWords;
   p.parts = h->parts.p;
   p.constVec = h->constVec.p;
   p.lutTable = h->lutTable.p;
@@ -201,32 +203,60 @@ void configure(tgs_sim *h) {
   h->lc.spw = int(h->spw);
   h->lc.G = G;
   h->lc.threads = NW * 32;
-  h->lc.smem = kLutTablePadded + size_t(h->img.maxVpSlots) * size_t(G) * 4;
   h->lc.stream = h->stream;
   void *fn = cycleKernelFor(int(h->spw), G);
-  if (h->lc.smem > size_t(h->props.sharedMemPerBlockOptin))
-    throw Error(TGS_ERR_RESOURCES, "value pool of " + std::to_string(h->img.maxVpSlots) + " slots x " + std::to_string(G) +
-                                       " groups needs " + std::to_string(h->lc.smem) + " B of shared memory; lower groups_per_item");
-  TGS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
-  int perSM = 0;
-  TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, int(h->lc.threads), h->lc.smem));
-  if (perSM <= 0) throw Error(TGS_ERR_RESOURCES, "no block of the cycle kernel fits on an SM with this configuration");
-  if (o.blocks_per_sm) perSM = std::min<int>(perSM, int(o.blocks_per_sm));
+  const size_t vpBytes = size_t(h->img.maxVpSlots) * size_t(G) * 4;
   const uint32_t nGB = h->gpad / uint32_t(G);
   size_t maxItems = 1;
   for (auto &r : h->design.regionPartitionIds) maxItems = std::max(maxItems, r.size() * nGB);
-  h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
 
-  // schedule (greedy gate count or learned cost)
+  // schedule (greedy gate count or learned cost); exec-level blocks are
+  // staged through shared memory when two of the largest fit next to the
+  // value pool (option resident_netlist = 2 disables staging)
   std::vector<std::vector<std::vector<float>>> cost;
   const std::vector<std::vector<std::vector<float>>> *costPtr = nullptr;
   if (o.schedule == TGS_SCHED_LEARNED && h->model && h->model->trained()) {
     h->model->predictAll(h->img, cost);
     costPtr = &cost;
   }
+  const size_t optin = size_t(h->props.sharedMemPerBlockOptin);
+  auto shape = [&](uint32_t stage) {
+    h->lc.smem = kLutTablePadded + 2 * size_t(stage) * 4 + vpBytes;
+    if (h->lc.smem > optin) return 0;
+    TGS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
+    int perSM = 0;
+    TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, int(h->lc.threads), h->lc.smem));
+    if (o.blocks_per_sm) perSM = std::min<int>(perSM, int(o.blocks_per_sm));
+    return perSM;
+  };
+  if (kLutTablePadded + vpBytes > optin)
+    throw Error(TGS_ERR_RESOURCES, "value pool of " + std::to_string(h->img.maxVpSlots) + " slots x " + std::to_string(G) +
+                                       " groups needs " + std::to_string(kLutTablePadded + vpBytes) +
+                                       " B of shared memory; lower groups_per_item");
+  // first pass to learn the largest level block (independent of the block count)
+  buildSchedule(h->design, h->img, NW, costPtr, 1, nGB, h->sched);
+  uint32_t stage = o.resident_netlist == 2 ? 0u : std::min<uint32_t>(h->sched.maxLevelWords, 4096u);
+  int perSM = shape(stage);
+  const int perSMNoStage = shape(0);
+  if (stage && perSM < std::max(1, perSMNoStage / 2)) {  // keep at least half the occupancy
+    stage = std::min<uint32_t>(stage, 1024u);
+    perSM = shape(stage);
+    if (perSM <= 0) {
+      stage = 0;
+      perSM = shape(0);
+    }
+  } else if (stage && perSM <= 0) {
+    stage = 0;
+    perSM = shape(0);
+  }
+  perSM = shape(stage);  // leaves the kernel attribute at the chosen size
+  if (perSM <= 0) throw Error(TGS_ERR_RESOURCES, "no block of the cycle kernel fits on an SM with this configuration");
+  h->stageWords = stage;
+  h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
   buildSchedule(h->design, h->img, NW, costPtr, h->lc.blocks, nGB, h->sched);
   h->parts.upload(h->img.parts, h->stream);
   h->schedW.upload(h->sched.words, h->stream);
+  h->levelDesc.upload(h->sched.levelDesc, h->stream);
   h->items.upload(h->sched.items, h->stream);
   h->itemBegin.upload(h->sched.itemBegin, h->stream);
 
