@@ -47,6 +47,8 @@ def args_parse():
     p.add_argument("--groups", type=int, default=4)
     p.add_argument("--warps", type=int, default=8)
     p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
+    p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
+    p.add_argument("--slots", type=int, default=0, help="resident slots for queued streams of uneven length")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cycles", type=int, default=1)
     p.add_argument("--out", default="")
@@ -255,6 +257,47 @@ def run_reference_gpu(a, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
+    """Streams of log-uniform length queued onto resident slots (retired and
+    admitted in place inside one persistent launch).  One step = the whole job."""
+    from toucangpurt_gb300 import sim, workloads
+
+    s = sim.Simulator(n_streams=8, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule)
+    s.init(gpu, dp, sp, False, False)
+    cyc = workloads.stream_lengths(a.workload, streams, seed=7 + rank)
+    stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], workloads.toggles(a.workload, info["pi_bits"]))
+    for _ in range(a.warmup):
+        s.batch_run(cyc, stim, rolling=False, slots=a.slots)
+    barrier(ws)
+    clk = Clocks(gpu)
+    dev_ms, t0 = 0.0, time.perf_counter()
+    for _ in range(a.steps):
+        out = s.batch_run(cyc, stim, rolling=False, slots=a.slots)
+        dev_ms += out.device_ms
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    st = s.design_stats()
+    total = allreduce_sum(float(cyc.sum()) * a.steps, ws)
+    dev_s = allreduce_max(dev_ms / 1000.0, ws)
+    wall_s = allreduce_max(wall, ws)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": total / dev_s, "unit": "stimulus-cycles/s", "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1000 * dev_s / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
+            "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
+                                   f"(mean {cyc.mean():.0f}), {st['streams_per_word'] * 0 + (a.slots or min(streams, 1024))} slots",
+                       "stream_cycles": int(cyc.sum()), "blocks": st["blocks"], "threads_per_block": st["threads"],
+                       "groups_per_item": st["groups_per_item"]},
+            "lut_evals_per_s": total / dev_s * st["lut_ops"],
+            "e2e": {"value": total / wall_s, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": int(cyc.nbytes),
+                    "d2h_bytes_per_step": int(streams * 8 * 3)},
+            "gpu_launches": a.steps, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    s.cleanup()
+
+
 def run_gb300(a, rank, ws):
     from toucangpurt_gb300 import build, sim, workloads
 
@@ -265,7 +308,10 @@ def run_gb300(a, rank, ws):
     streams = a.streams or workloads.RUNS[a.workload]["streams"]
     cps = a.cycles_per_step or (200 if a.workload in ("largest", "learned") else 2000)
     schedule = 1 if a.schedule == "learned" else 0
-    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule)
+    if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
+        return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
+    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule,
+                      resident_netlist=2 if a.no_stage else 0)
     s.init(gpu, dp, sp, False, False)
     st = s.design_stats()
     toggle = workloads.toggles(a.workload, info["pi_bits"])

@@ -163,11 +163,17 @@ typedef struct tgs_stimulus {
   const uint32_t *reg;     /* regPool nibble ids */
   const uint8_t *bits;     /* bit width of each input nibble (1..4) */
   const uint16_t *toggle;  /* NULL = all inputs uniform */
+  /* Optional host table of input values, [cycle][input][stream] one nibble
+   * per byte, covering the cycles of this call (runs where every stream is
+   * resident and equally long); replaces the seeded values.  Pinned memory
+   * (tgs_host_alloc) makes the upload faster. */
+  const uint8_t *table;
 } tgs_stimulus;
 
 #define TGS_BATCH_CYCLE_DIGESTS 1u /* fill cycle_digest[] */
 #define TGS_BATCH_ROLLING 2u       /* fill rolling_digest[] */
 #define TGS_BATCH_FINAL_STATE 4u   /* fill final_regs[] / final_mems[] */
+#define TGS_BATCH_CONTINUE 8u      /* continue every stream from the previous call's state and cycle */
 
 typedef struct tgs_batch {
   uint32_t n_streams;       /* streams in the job (may exceed resident slots) */
@@ -191,10 +197,18 @@ typedef struct tgs_batch_result {
   uint32_t launches;          /* kernel launches issued */
 } tgs_batch_result;
 
-/* Runs every stream of the job from the initial state.  Streams beyond the
- * resident slots are queued; a slot whose stream finished is refilled in
- * place by the next queued stream. */
+/* Runs every stream of the job from the initial state.  With equal lengths
+ * and all streams resident, one launch runs them side by side.  Otherwise
+ * the streams are queued onto `slots` resident slots (default min(n, 1024)):
+ * a slot whose stream finished is retired and refilled in place by the next
+ * queued stream inside the same persistent launch (final digests, rolling
+ * digests, per-cycle digests and stop cycles are reported per job stream;
+ * final_regs / final_mems are not available in that form). */
 int tgs_batch_run(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res);
+
+/* Page-locked host memory for stimulus tables and results. */
+int tgs_host_alloc(size_t bytes, void **out);
+int tgs_host_free(void *p);
 
 /* ---- design statistics and launch shape (new) ------------------------- */
 typedef struct tgs_design_stats {

@@ -28,7 +28,7 @@ STABLE = {
     "powerlaw": (dict(seed=12, n_lut=20000, levels=12, operands=3, palette_pct=40, fanout_alpha=2.2, max_fanout=64,
                       ff_bits=2048, pi_bits=64, n_vec_ops=24, vec_nibbles=8, n_mems=3, mem_depth=4096, mem_width=32,
                       mem_read_ports=2, mem_write_ports=2, mem_multi_writer=1, luts_per_part=2500, cone_depth=2),
-                 "5c74132c2b8657d2"),
+                 "cd639344cc83bac5"),
 }
 
 

@@ -25,7 +25,7 @@ ERR_RESOURCES, ERR_TIMEOUT, ERR_STATE, ERR_NOT_FOUND, ERR_RANGE, ERR_DEVICE_FAUL
 
 SCHED_GREEDY, SCHED_LEARNED = 0, 1
 MODE_PERSISTENT, MODE_GRAPH = 0, 1
-BATCH_CYCLE_DIGESTS, BATCH_ROLLING, BATCH_FINAL_STATE = 1, 2, 4
+BATCH_CYCLE_DIGESTS, BATCH_ROLLING, BATCH_FINAL_STATE, BATCH_CONTINUE = 1, 2, 4, 8
 
 
 class TgsError(RuntimeError):
@@ -46,6 +46,7 @@ class Options(C.Structure):
 class Stimulus(C.Structure):
     _fields_ = [
         ("base_seed", C.c_uint64), ("n_inputs", C.c_uint32), ("reg", u32p), ("bits", u8p), ("toggle", u16p),
+        ("table", u8p),
     ]
 
 
@@ -131,6 +132,8 @@ SIGNATURES = {
     "tgs_pool_digests_noalloc": [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint32, u64p],
     "tgs_batch_run": [C.c_void_p, C.POINTER(Batch), C.POINTER(BatchResult)],
     "tgs_get_design_stats": [C.c_void_p, C.POINTER(DesignStats)],
+    "tgs_host_alloc": [C.c_size_t, C.POINTER(C.c_void_p)],
+    "tgs_host_free": [C.c_void_p],
     "tgs_default_gen_config": [C.POINTER(GenConfig)],
     "tgs_generate": [C.POINTER(GenConfig), C.c_char_p, C.c_char_p, C.POINTER(GenInfo)],
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],

@@ -364,7 +364,7 @@ __device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t 
 // ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
 template <int SPW, int G>
 __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__ vp, const uint8_t *__restrict__ tab,
-                         Stage &st, uint32_t cycle) {
+                         Stage &st, uint32_t cycle, const uint32_t *retire) {
   const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
   const PartDesc &d = p.parts[pid];
   const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
@@ -424,7 +424,20 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
   __syncthreads();
 
   // last level (evalLastLevel / evalLastLevelExgWrite, SimEval.cu:625-761)
-  if (d.copyKind) {
+  // masks of streams retiring this cycle (admission): their registers take
+  // the initial values, their memory writes / prints / stops are dropped
+  uint32_t rm[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) rm[g] = retire ? __ldcg(retire + gb * G + g) : 0u;
+  if (d.copyKind == 1 && retire) {
+    for (uint32_t i = tid; i < d.copySlots; i += nthr) {
+      const uint32_t iv = p.initRegs[d.copyDst + i];
+      const uint32_t init = SPW == 8 ? rep8(iv) : iv;
+      uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
+#pragma unroll
+      for (int g = 0; g < G; ++g) dst[g] = (vp[(d.copySrc + i) * G + g] & ~rm[g]) | (init & rm[g]);
+    }
+  } else if (d.copyKind) {
     uint32_t *pool = d.copyKind == 1 ? p.regs : p.exg;
     for (uint32_t i = tid; i < d.copySlots; i += nthr)
       copyOutG<G>(pool + size_t(d.copyDst + i) * p.gpad + gb * G, vp + (d.copySrc + i) * G);
@@ -437,7 +450,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
       const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
       const bool multi = (hi >> 31) != 0;
       const uint32_t av = w2 & 0xFFFFu, dat = w2 >> 16;
-      const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+      const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
       const uint32_t DAT = dat < 16 ? rep8(dat) : vp[dat * G + g];
       uint32_t AD[8];
 #pragma unroll
@@ -462,7 +475,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
       for (uint32_t i = tid; i < d.printCount * G; i += nthr) {
         const uint32_t w = __ldg(p.net + d.printOff + i / G), g = i % G;
         const uint32_t en = w & 0xFFFFu, msg = w >> 16;
-        const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+        const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
         for (int k = 0; k < SPW; ++k) {
           const uint32_t s = (gb * G + g) * SPW + k;
           if (s < p.nStreams && nib(EN, k) != 0 && msg < p.nPrintMsgs) printf("%s", p.printMsgs[msg]);
@@ -472,7 +485,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
       const uint32_t opi = i / G, g = i % G;
       const uint32_t en = __ldg(p.net + d.stopOff + opi);
-      const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+      const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
       for (int k = 0; k < SPW; ++k) {
         const uint32_t s = (gb * G + g) * SPW + k;
         if (s >= p.nStreams || nib(EN, k) == 0) continue;
@@ -495,6 +508,34 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
 }
 
 // ---- stimulus / digests ------------------------------------------------------
+// Value of input `inp` of slot s for global cycle `cycle`; false when the slot
+// takes no input that cycle (idle, past its stream's end, or a padding slot).
+__device__ __forceinline__ bool stimValue(const KParams &p, uint32_t s, uint32_t cycle, uint32_t inp, uint32_t cur,
+                                          uint32_t mask, uint32_t tog, uint32_t &v) {
+  uint32_t lc;
+  unsigned long long seed;
+  if (s >= p.nStreams) return false;  // padding slot of the last group
+  if (p.flags & kFlagSlots) {
+    const uint32_t q = __ldcg(p.slotStream + s);
+    if (q == kNoStream || cycle >= __ldcg(p.slotRetire + s)) return false;
+    lc = cycle - __ldcg(p.slotStart + s);
+    seed = __ldg(p.jobSeed + q);
+  } else {
+    lc = cycle;
+    seed = __ldg(p.streamSeed + s);
+    if (p.stimTable) {
+      v = __ldg(p.stimTable + (size_t(cycle - p.stimTableC0) * p.nStim + inp) * p.nStreams + s) & mask;
+      return true;
+    }
+  }
+  const unsigned long long h = dmix64(seed ^ dmix64((unsigned long long)lc << 32 | inp));
+  if (tog == 0)
+    v = uint32_t(h) & mask;
+  else
+    v = (h >> 48) < tog ? cur ^ mask : cur;
+  return true;
+}
+
 template <int SPW>
 __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
   const uint32_t total = p.nStim * p.gpad;
@@ -506,33 +547,42 @@ __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, u
     uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
     const uint32_t w = __ldcg(wp);
     uint32_t nw = 0;
-    const unsigned long long key = dmix64((unsigned long long)cycle << 32 | inp);
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
-      const uint32_t s = g * SPW + k;
       const uint32_t cur = nib(w, k);
       uint32_t v = cur;
-      if (s < p.nStreams) {
-        const unsigned long long h = dmix64(__ldg(p.streamSeed + s) ^ key);
-        if (tog == 0)
-          v = uint32_t(h) & mask;
-        else if ((h >> 48) < tog)
-          v = cur ^ mask;
-      }
+      stimValue(p, g * SPW + k, cycle, inp, cur, mask, tog, v);
       nw |= v << (4 * k);
     }
     *wp = nw;
   }
 }
 
+// Streams whose register digest this cycle contributes: every active stream
+// with per-cycle digests, else (admission) only the streams retiring now.
+__device__ __forceinline__ bool digestStream(const KParams &p, uint32_t s, uint32_t cycle) {
+  if (s >= p.nStreams) return false;
+  if (!(p.flags & kFlagSlots)) return true;
+  if (__ldcg(p.slotStream + s) == kNoStream) return false;
+  return (p.flags & kFlagDigest) || __ldcg(p.slotRetire + s) == cycle;
+}
+
 // Per-cycle register digest: sum over i of mix64(i << 8 | nibble), per stream.
 template <int SPW>
-__device__ void digestSlice(const KParams &p) {
+__device__ void digestSlice(const KParams &p, uint32_t cycle) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
   const uint32_t chunks = (p.regSlots + 255) / 256;
   const uint32_t units = chunks * p.gpad;
   for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
     const uint32_t g = u % p.gpad, ch = u / p.gpad;
+    bool want[SPW];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) {
+      want[k] = digestStream(p, g * SPW + k, cycle);
+      any |= want[k];
+    }
+    if (!any) continue;
     unsigned long long acc[SPW];
 #pragma unroll
     for (int k = 0; k < SPW; ++k) acc[k] = 0;
@@ -546,18 +596,106 @@ __device__ void digestSlice(const KParams &p) {
     for (int k = 0; k < SPW; ++k) {
       unsigned long long a = acc[k];
       for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-      const uint32_t s = g * SPW + k;
-      if (lane == 0 && s < p.nStreams) atomicAdd(p.digAcc + s, a);
+      if (lane == 0 && want[k]) atomicAdd(p.digAcc + g * SPW + k, a);
     }
   }
 }
 
 __device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
   for (uint32_t s = gtid; s < p.nStreams; s += gthreads) {
+    uint32_t q = s, lc = cycle - p.cycBase;
+    if (p.flags & kFlagSlots) {
+      q = __ldcg(p.slotStream + s);
+      if (q == kNoStream || __ldcg(p.slotRetire + s) == cycle) continue;  // retiring: kept for the admin phase
+      lc = cycle - __ldcg(p.slotStart + s);
+    }
     const unsigned long long dg = __ldcg(p.digAcc + s);
     p.digAcc[s] = 0;
     p.roll[s] = dmix64(p.roll[s] + dg);
-    if (p.cycDig && cycle < p.cycStride) p.cycDig[size_t(s) * p.cycStride + cycle] = dg;
+    if (p.cycDig && lc < p.cycStride) p.cycDig[size_t(q) * p.cycStride + lc] = dg;
+  }
+}
+
+// ---- admission events --------------------------------------------------------
+// Region 0 of a retire cycle: mark the retiring slots and digest their memories.
+template <int SPW>
+__device__ void eventRegion0(const KParams &p, uint32_t ev) {
+  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
+  if (blockIdx.x == 0)
+    for (uint32_t j = eb + threadIdx.x; j < ee; j += blockDim.x) {
+      const uint32_t s = __ldg(p.eventSlot + j);
+      atomicOr(p.retireMask + s / SPW, 15u << (4 * (s % SPW)));
+    }
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  const uint32_t chunk = 8192, chunks = (p.memPoolSize + chunk - 1) / chunk;
+  const uint32_t units = (ee - eb) * chunks;
+  for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
+    const uint32_t s = __ldg(p.eventSlot + eb + u / chunks), ch = u % chunks;
+    const uint8_t *m = p.mems + s * p.memStride;
+    unsigned long long a = 0;
+    const uint32_t end = min(p.memPoolSize, (ch + 1) * chunk);
+    for (uint32_t i = ch * chunk + lane; i < end; i += 32) a += dmix64((unsigned long long)i << 8 | __ldcg(m + i));
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    if (lane == 0) atomicAdd(p.memAcc + s, a);
+  }
+}
+
+// Region 1 of a retire cycle: reset the retiring slots' memories (their
+// memory writes are dropped this cycle).
+__device__ void eventRegion1(const KParams &p, uint32_t ev, uint32_t gtid, uint32_t gthreads) {
+  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
+  const uint32_t vecs = uint32_t((p.memPoolSize + 15ull) / 16);
+  const size_t total = size_t(ee - eb) * vecs;
+  for (size_t i = gtid; i < total; i += gthreads) {
+    const uint32_t s = __ldg(p.eventSlot + eb + uint32_t(i / vecs));
+    const size_t v = i % vecs;
+    reinterpret_cast<uint4 *>(p.mems + s * p.memStride)[v] = __ldg(reinterpret_cast<const uint4 *>(p.initMems) + v);
+  }
+}
+
+// After the region-1 barrier: publish the retired streams' results and admit
+// the next queued stream into each slot (with its cycle-0 inputs).
+template <int SPW>
+__device__ void eventAdmit(const KParams &p, uint32_t ev, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
+  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
+  for (uint32_t j = eb + gtid; j < ee; j += gthreads) {
+    const uint32_t s = __ldg(p.eventSlot + j), qn = __ldg(p.eventNext + j);
+    const uint32_t q = __ldcg(p.slotStream + s), start = __ldcg(p.slotStart + s);
+    p.outReg[q] = __ldcg(p.digAcc + s);
+    p.outMem[q] = __ldcg(p.memAcc + s);
+    p.outRoll[q] = __ldcg(p.roll + s);
+    const uint32_t sc = __ldcg(p.stopCycle + s);
+    p.outStop[q] = sc == 0xFFFFFFFFu ? sc : sc - start;
+    p.digAcc[s] = 0;
+    p.memAcc[s] = 0;
+    p.roll[s] = 0;
+    p.stop[s] = 0;
+    p.stopCycle[s] = 0xFFFFFFFFu;
+    const uint32_t g = s / SPW, k = s % SPW;
+    atomicAnd(p.retireMask + g, ~(15u << (4 * k)));
+    if (qn == kNoStream) {
+      p.slotStream[s] = kNoStream;
+      continue;
+    }
+    p.slotStream[s] = qn;
+    p.slotStart[s] = cycle + 1;
+    p.slotRetire[s] = cycle + 1 + __ldg(p.jobLen + qn);
+    // primary inputs restart from the initial register values
+    for (uint32_t inp = 0; inp < p.nStim; ++inp) {
+      const uint32_t reg = __ldg(p.stimReg + inp);
+      const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
+      const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
+      const uint32_t cur = p.initRegs[reg] & 15u;
+      uint32_t v = cur;
+      const unsigned long long h = dmix64(__ldg(p.jobSeed + qn) ^ dmix64((unsigned long long)0 << 32 | inp));
+      if (tog == 0)
+        v = uint32_t(h) & mask;
+      else
+        v = (h >> 48) < tog ? cur ^ mask : cur;
+      uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
+      atomicAnd(wp, ~(15u << (4 * k)));
+      atomicOr(wp, v << (4 * k));
+    }
   }
 }
 
@@ -654,7 +792,10 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
     applyStimulus<SPW>(p, c0, gtid, gthreads);
     if (!gridSync(p, gen)) return;
   }
+  uint32_t ev = 0;
+  const bool slots = (p.flags & kFlagSlots) != 0;
   for (uint32_t t = c0; t < c0 + nCycles; ++t) {
+    const bool event = slots && ev < p.nEvents && __ldg(p.events + ev) == t;
 #pragma unroll 1
     for (uint32_t r = 0; r < 2; ++r) {
       const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
@@ -663,7 +804,7 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
       for (uint32_t i = b; i < e; ++i) {
         const long long t0 = clock64();
         const uint32_t item = __ldg(p.items + i);
-        evalItem<SPW, G>(p, item, vp, tab, st, t);
+        evalItem<SPW, G>(p, item, vp, tab, st, t, (event && r == 1) ? p.retireMask : nullptr);
         // per-partition clock64 profile (SimEval.cu:894-983): running mean of
         // the useful ticks over cycles [100, 200) of group block 0
         if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {
@@ -672,8 +813,10 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
           p.profUseful[pid] = (p.profUseful[pid] * pc + useful) / (pc + 1);
         }
       }
-      if (r == 0 && (p.flags & kFlagDigest)) digestSlice<SPW>(p);
+      if (r == 0 && ((p.flags & kFlagDigest) || event)) digestSlice<SPW>(p, t);
+      if (r == 0 && event) eventRegion0<SPW>(p, ev);
       if (r == 1) {
+        if (event) eventRegion1(p, ev, gtid, gthreads);
         if ((p.flags & kFlagStimulus) && t + 1 < c0 + nCycles) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
         if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
       }
@@ -688,6 +831,11 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
           p.profTotal[pid] = (p.profTotal[pid] * pc + total) / (pc + 1);
         }
       }
+    }
+    if (event) {
+      eventAdmit<SPW>(p, ev, t, gtid, gthreads);
+      ++ev;
+      if (!gridSync(p, gen)) return;
     }
     if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
   }

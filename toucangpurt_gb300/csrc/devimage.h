@@ -104,20 +104,40 @@ struct KParams {
   uint32_t nBlocks;
   uint32_t nParts;
   uint32_t cycStride;
+  uint32_t cycBase;           // cycle of index 0 in cycDig rows (direct runs)
   uint32_t enablePrint;
   uint32_t flags;             // kFlag*
   uint32_t printDiag;         // reference-style first-stop diagnostics (single stream)
   unsigned long long timeoutNs;
   const char *const *printMsgs;
   uint32_t nPrintMsgs;
-  uint32_t pad0;
+  uint32_t stimTableC0;       // first cycle the stimulus table covers
+  const uint8_t *stimTable;   // [cycle][input][stream] nibbles, or null (hash stimulus)
+  // admission (kFlagSlots): queued job streams run on the resident slots
+  uint32_t *slotStream;       // [slots] job stream, kNoStream when idle
+  uint32_t *slotStart;        // [slots] global cycle of the stream's cycle 0
+  uint32_t *slotRetire;       // [slots] global cycle at which it retires (start + length)
+  const uint32_t *jobLen;     // [jobs]
+  const unsigned long long *jobSeed;  // [jobs]
+  const uint32_t *events;     // [nEvents] global cycles with retirements, increasing
+  const uint32_t *eventBegin; // [nEvents + 1] into eventSlot / eventNext
+  const uint32_t *eventSlot;  // retiring slot
+  const uint32_t *eventNext;  // job stream admitted into it, kNoStream for none
+  uint32_t *retireMask;       // [gpad] nibble masks of the current event's slots
+  unsigned long long *memAcc; // [slots] final memory digests
+  unsigned long long *outReg, *outMem, *outRoll;  // [jobs]
+  uint32_t *outStop;          // [jobs]
+  uint32_t nEvents, nJobs;
 };
+
+constexpr uint32_t kNoStream = 0xFFFFFFFFu;
 
 enum : uint32_t {
   kFlagStimulus = 1u,   // apply the stimulus before every cycle
   kFlagDigest = 2u,     // per-cycle register digests (rolling / per-cycle array)
   kFlagProfile = 4u,    // per-partition clock64 profile (free-running)
-  kFlagCountCycles = 8u // advance realCycles (free-running launches only, SimEval.cu:985-989)
+  kFlagCountCycles = 8u, // advance realCycles (free-running launches only, SimEval.cu:985-989)
+  kFlagSlots = 16u       // job streams queued onto resident slots, retired and admitted in place
 };
 
 enum : uint32_t {

@@ -284,7 +284,8 @@ class PartGen {
   // Popularity weights follow a discrete power law: weight 2^k with
   // P(k) proportional to 2^(-k (alpha - 1)), k = 0 .. log2(maxFan), so that
   // P(weight >= x) ~ x^-(alpha - 1).  Only integers after one rounding of the
-  // class ratio to 32-bit fixed point: designs are identical on every host.
+  // exponent to 1/64: integer arithmetic only, so designs are identical on every
+  // host (x86-64 and aarch64 libm / FMA contraction would otherwise differ).
   void weigh(Band &b) {
     b.cum.resize(b.vals.size());
     uint64_t acc = 0;
@@ -298,7 +299,11 @@ class PartGen {
     if (classThr_.empty()) {
       uint32_t kmax = 0;
       while ((2u << kmax) <= std::max<uint32_t>(1, k_.maxFan)) ++kmax;
-      const uint64_t ratio = uint64_t(std::llround(std::exp2(-(k_.alpha - 1.0)) * 4294967296.0));  // Q32
+      // ratio = 2^-(alpha - 1) in Q32 as (2^-1/64)^steps, alpha - 1 rounded to 1/64
+      constexpr uint64_t kTwoPowMinusSixtyFourth = 4248701965ull;  // 2^(-1/64) in Q32
+      const int64_t steps = std::max<int64_t>(0, (int64_t)((k_.alpha - 1.0) * 64.0 + 0.5));
+      uint64_t ratio = uint64_t(1) << 32;
+      for (int64_t i = 0; i < steps; ++i) ratio = (ratio * kTwoPowMinusSixtyFourth) >> 32;
       std::vector<uint64_t> p(kmax + 1);
       p[0] = uint64_t(1) << 32;
       for (uint32_t k = 1; k <= kmax; ++k) p[k] = (p[k - 1] * ratio) >> 32;
@@ -392,7 +397,10 @@ class PartGen {
     else if (three)
       a = lane();
     ++cnt_.lut;
-    return CGMicroPartLUTMiddleLevelOp(lut, a, lane(), lane());
+    // draws in a fixed order (argument evaluation order is unspecified)
+    const uint8_t b = lane();
+    const uint8_t c = lane();
+    return CGMicroPartLUTMiddleLevelOp(lut, a, b, c);
   }
 
   Rng &rng_;

@@ -15,6 +15,8 @@
 #include <fstream>
 #include <iterator>
 #include <memory>
+#include <queue>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -101,6 +103,11 @@ struct tgs_sim {
   tgs::DBuf<char *> msgPtrs;
   std::vector<tgs::DBuf<char>> msgs;
   tgs::DBuf<uint32_t> ioIds;
+  tgs::DBuf<uint32_t> slotStream, slotStart, slotRetire, jobLen, events, eventBegin, eventSlot, eventNext, retireMask,
+      outStop;
+  tgs::DBuf<unsigned long long> jobSeed, memAcc, outReg, outMem, outRoll;
+  tgs::DBuf<uint8_t> stimTable;
+  uint64_t batchCycle = 0;  // cycles run by TGS_BATCH_CONTINUE batches since the last reset
   tgs::DBuf<uint8_t> ioBytes;
   tgs::KParams kp{};
   // learned cost model (optional)
@@ -312,7 +319,9 @@ void upload(tgs_sim *h) {
   std::vector<uint8_t> ir(std::max<uint32_t>(4, (h->design.regPoolSize + 3) & ~3u), 0);
   std::memcpy(ir.data(), h->design.regPool.data(), h->design.regPool.size());
   h->initRegs.upload(ir, s);
-  h->initMems.alloc(std::max<size_t>(16, h->design.memPool.size()));
+  // rounded up to 16 bytes: the in-kernel memory reset copies 16-byte vectors
+  h->initMems.alloc(std::max<size_t>(16, (h->design.memPool.size() + 15) & ~size_t(15)));
+  TGS_CUDA(cudaMemsetAsync(h->initMems.p, 0, h->initMems.n, s));
   if (!h->design.memPool.empty())
     TGS_CUDA(cudaMemcpyAsync(h->initMems.p, h->design.memPool.data(), h->design.memPool.size(), cudaMemcpyHostToDevice, s));
   h->err.alloc(1);
@@ -703,6 +712,7 @@ int tgs_reset_state(tgs_sim *h) {
     requireLoaded(h);
     resetState(h);
     h->cycleCnt = 0;
+    h->batchCycle = 0;
   });
 }
 
@@ -777,71 +787,37 @@ int tgs_validate_file(const char *design_path, const char *symbol_path, uint64_t
 
 namespace tgs {
 
-// Streams of a job run from the initial state for cycles[s] cycles each, all
-// resident at once (the current slot count must hold the job).
-void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
-  if (!job || !job->cycles || job->n_streams == 0) throw Error(TGS_ERR_ARG, "empty batch");
-  const uint32_t n = job->n_streams;
-  uint32_t cyc = job->cycles[0];
-  for (uint32_t s = 1; s < n; ++s)
-    if (job->cycles[s] != cyc) throw Error(TGS_ERR_ARG, "streams of unequal length need resident slots < n_streams");
-  if (h->opt.n_streams != n) {
-    h->opt.n_streams = n;
-    configure(h);
+namespace {
+
+void checkStimulus(tgs_sim *h, const tgs_stimulus *st) {
+  for (auto &pd : h->img.parts)
+    if (pd.copyKind == 1)
+      for (uint32_t i = 0; i < st->n_inputs; ++i)
+        if (st->reg[i] >= pd.copyDst && st->reg[i] < pd.copyDst + pd.copySlots)
+          throw Error(TGS_ERR_ARG, "stimulus register " + std::to_string(st->reg[i]) + " is written by the design");
+  for (uint32_t i = 0; i < st->n_inputs; ++i) {
+    if (st->reg[i] >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "stimulus register beyond regPool");
+    if (st->bits[i] < 1 || st->bits[i] > 4) throw Error(TGS_ERR_RANGE, "stimulus bit width outside 1..4");
   }
-  const tgs_stimulus *st = job->stim;
-  uint32_t flags = 0;
-  if (st && st->n_inputs) {
-    flags |= kFlagStimulus;
-    // primary inputs must not be targets of a partition's register copy
-    for (auto &pd : h->img.parts)
-      if (pd.copyKind == 1)
-        for (uint32_t i = 0; i < st->n_inputs; ++i)
-          if (st->reg[i] >= pd.copyDst && st->reg[i] < pd.copyDst + pd.copySlots)
-            throw Error(TGS_ERR_ARG, "stimulus register " + std::to_string(st->reg[i]) + " is written by the design");
-    for (uint32_t i = 0; i < st->n_inputs; ++i) {
-      if (st->reg[i] >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "stimulus register beyond regPool");
-      if (st->bits[i] < 1 || st->bits[i] > 4) throw Error(TGS_ERR_RANGE, "stimulus bit width outside 1..4");
-    }
-    h->stimReg.upload(st->reg, st->n_inputs, h->stream);
-    h->stimBits.upload(st->bits, st->n_inputs, h->stream);
-    if (st->toggle) h->stimToggle.upload(st->toggle, st->n_inputs, h->stream);
-    std::vector<unsigned long long> seeds(n);
-    for (uint32_t s = 0; s < n; ++s) seeds[s] = mix64(st->base_seed ^ s);
-    h->seeds.upload(seeds, h->stream);
+}
+
+// Stimulus and digests run beside the regions: registers must be read-only
+// in region 0 and unread in region 1.
+void checkRegionRoles(tgs_sim *h) {
+  for (auto &pd : h->img.parts) {
+    if (pd.region == 0 && pd.copyKind == 1)
+      throw Error(TGS_ERR_INVALID_DESIGN, "region 0 writes registers: stimulus/digest runs need region-0 register writes to be absent");
+    if (pd.region == 1 && pd.l0Exchange == 0 && pd.l0Count)
+      throw Error(TGS_ERR_INVALID_DESIGN, "region 1 reads registers: stimulus/digest runs need region 1 to read only the exchange pool");
   }
-  const bool wantDigest = (job->flags & (TGS_BATCH_CYCLE_DIGESTS | TGS_BATCH_ROLLING)) != 0;
-  if (wantDigest) flags |= kFlagDigest;
-  if (flags) {
-    // stimulus and digests run beside the regions: registers must be
-    // read-only in region 0 and unread in region 1
-    for (auto &pd : h->img.parts) {
-      if (pd.region == 0 && pd.copyKind == 1) throw Error(TGS_ERR_INVALID_DESIGN, "region 0 writes registers: stimulus/digest runs need region-0 register writes to be absent");
-      if (pd.region == 1 && pd.l0Exchange == 0 && pd.l0Count) throw Error(TGS_ERR_INVALID_DESIGN, "region 1 reads registers: stimulus/digest runs need region 1 to read only the exchange pool");
-    }
-  }
-  resetState(h);
-  fillParams(h);
-  KParams &p = h->kp;
-  p.nStim = st ? st->n_inputs : 0;
-  p.stimReg = h->stimReg.p;
-  p.stimBits = h->stimBits.p;
-  p.stimToggle = (st && st->toggle) ? h->stimToggle.p : nullptr;
-  p.streamSeed = h->seeds.p;
-  TGS_CUDA(cudaMemsetAsync(h->digAcc.p, 0, n * 8, h->stream));
-  TGS_CUDA(cudaMemsetAsync(h->roll.p, 0, n * 8, h->stream));
-  const bool perCycle = (job->flags & TGS_BATCH_CYCLE_DIGESTS) && res && res->cycle_digest && res->cycle_stride;
-  if (perCycle) {
-    h->cycDig.alloc(size_t(n) * res->cycle_stride);
-    TGS_CUDA(cudaMemsetAsync(h->cycDig.p, 0, size_t(n) * res->cycle_stride * 8, h->stream));
-    p.cycDig = h->cycDig.p;
-    p.cycStride = res->cycle_stride;
-  }
+}
+
+float runTimed(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
   cudaEvent_t e0, e1;
   TGS_CUDA(cudaEventCreate(&e0));
   TGS_CUDA(cudaEventCreate(&e1));
   TGS_CUDA(cudaEventRecord(e0, h->stream));
-  runCycles(h, 0, cyc, flags);
+  runCycles(h, c0, n, flags);
   TGS_CUDA(cudaEventRecord(e1, h->stream));
   TGS_CUDA(cudaEventSynchronize(e1));
   float ms = 0;
@@ -850,37 +826,245 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   cudaEventDestroy(e1);
   TGS_CUDA(cudaStreamSynchronize(h->stream));
   checkDeviceError(h);
-  h->cycleCnt = cyc;
+  return ms;
+}
+
+// Admission: streams queued onto S resident slots.  The host simulates the
+// queue (every length is known up front): each retirement is an event
+// (global cycle, slot, next stream); the kernel follows the event list.
+void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uint32_t flags) {
+  const uint32_t n = job->n_streams;
+  uint32_t S = job->slots ? job->slots : std::min<uint32_t>(n, 1024);
+  S = std::min(S, n);
+  if (S > 1) S = (S + 7) / 8 * 8;
+  if (res && (res->final_regs || res->final_mems))
+    throw Error(TGS_ERR_ARG, "final_regs / final_mems need every stream resident (slots >= n_streams, equal lengths)");
+  if (job->stim && job->stim->table) throw Error(TGS_ERR_ARG, "stimulus tables need every stream resident and equally long");
+  for (uint32_t q = 0; q < n; ++q)
+    if (job->cycles[q] == 0) throw Error(TGS_ERR_ARG, "stream lengths must be at least one cycle");
+  // retiring streams' memories are digested in region 0 and reset in region 1
+  for (auto &pd : h->img.parts)
+    if (pd.region == 0 && pd.memWCount)
+      throw Error(TGS_ERR_INVALID_DESIGN, "region 0 writes memories: in-place admission needs memory writes in region 1 only");
+  if (h->opt.n_streams != S) {
+    h->opt.n_streams = S;
+    configure(h);
+  }
+  // queue simulation: min-heap of (retire cycle, slot)
+  std::vector<uint32_t> slotStream(S, kNoStream), slotStart(S, 0), slotRetire(S, 0xFFFFFFFFu);
+  using E = std::pair<uint64_t, uint32_t>;
+  std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
+  for (uint32_t s = 0; s < S && s < n; ++s) {
+    slotStream[s] = s;
+    slotRetire[s] = job->cycles[s];
+    pq.push({job->cycles[s], s});
+  }
+  std::vector<std::tuple<uint64_t, uint32_t, uint32_t>> evs;  // (cycle, slot, next)
+  uint32_t nextQ = std::min(S, n);
+  while (!pq.empty()) {
+    auto [t, s] = pq.top();
+    pq.pop();
+    uint32_t qn = kNoStream;
+    if (nextQ < n) {
+      qn = nextQ++;
+      pq.push({t + 1 + job->cycles[qn], s});
+    }
+    evs.emplace_back(t, s, qn);
+  }
+  std::sort(evs.begin(), evs.end());
+  const uint64_t last = std::get<0>(evs.back());
+  if (last >= 0xFFFFFFF0ull) throw Error(TGS_ERR_RANGE, "job too long for 32-bit cycle counters");
+  std::vector<uint32_t> events, eventBegin, eventSlot, eventNext;
+  for (size_t i = 0; i < evs.size(); ++i) {
+    if (events.empty() || events.back() != std::get<0>(evs[i])) {
+      events.push_back(uint32_t(std::get<0>(evs[i])));
+      eventBegin.push_back(uint32_t(i));
+    }
+    eventSlot.push_back(std::get<1>(evs[i]));
+    eventNext.push_back(std::get<2>(evs[i]));
+  }
+  eventBegin.push_back(uint32_t(evs.size()));
+  std::vector<uint32_t> lens(job->cycles, job->cycles + n);
+  std::vector<unsigned long long> seeds(n);
+  for (uint32_t q = 0; q < n; ++q) seeds[q] = mix64((job->stim ? job->stim->base_seed : 0) ^ q);
+
+  resetState(h);
+  fillParams(h);
+  KParams &p = h->kp;
+  cudaStream_t st = h->stream;
+  h->slotStream.upload(slotStream, st);
+  h->slotStart.upload(slotStart, st);
+  h->slotRetire.upload(slotRetire, st);
+  h->jobLen.upload(lens, st);
+  h->jobSeed.upload(seeds, st);
+  h->events.upload(events, st);
+  h->eventBegin.upload(eventBegin, st);
+  h->eventSlot.upload(eventSlot, st);
+  h->eventNext.upload(eventNext, st);
+  h->retireMask.alloc(h->gpad);
+  h->memAcc.alloc(S);
+  h->outReg.alloc(n);
+  h->outMem.alloc(n);
+  h->outRoll.alloc(n);
+  h->outStop.alloc(n);
+  TGS_CUDA(cudaMemsetAsync(h->retireMask.p, 0, h->gpad * 4, st));
+  TGS_CUDA(cudaMemsetAsync(h->memAcc.p, 0, S * 8ull, st));
+  TGS_CUDA(cudaMemsetAsync(h->digAcc.p, 0, S * 8ull, st));
+  TGS_CUDA(cudaMemsetAsync(h->roll.p, 0, S * 8ull, st));
+  p.slotStream = h->slotStream.p;
+  p.slotStart = h->slotStart.p;
+  p.slotRetire = h->slotRetire.p;
+  p.jobLen = h->jobLen.p;
+  p.jobSeed = h->jobSeed.p;
+  p.events = h->events.p;
+  p.eventBegin = h->eventBegin.p;
+  p.eventSlot = h->eventSlot.p;
+  p.eventNext = h->eventNext.p;
+  p.retireMask = h->retireMask.p;
+  p.memAcc = h->memAcc.p;
+  p.outReg = h->outReg.p;
+  p.outMem = h->outMem.p;
+  p.outRoll = h->outRoll.p;
+  p.outStop = h->outStop.p;
+  p.nEvents = uint32_t(events.size());
+  p.nJobs = n;
+  p.streamSeed = h->jobSeed.p;
+  if (flags & kFlagStimulus) {
+    p.nStim = job->stim->n_inputs;
+    p.stimReg = h->stimReg.p;
+    p.stimBits = h->stimBits.p;
+    p.stimToggle = job->stim->toggle ? h->stimToggle.p : nullptr;
+  }
+  const bool perCycle = (job->flags & TGS_BATCH_CYCLE_DIGESTS) && res && res->cycle_digest && res->cycle_stride;
+  if (perCycle) {
+    h->cycDig.alloc(size_t(n) * res->cycle_stride);
+    TGS_CUDA(cudaMemsetAsync(h->cycDig.p, 0, size_t(n) * res->cycle_stride * 8, st));
+    p.cycDig = h->cycDig.p;
+    p.cycStride = res->cycle_stride;
+  }
+  const float ms = runTimed(h, 0, uint32_t(last) + 1, flags | kFlagSlots);
+  h->cycleCnt = last + 1;
+  if (!res) return;
+  uint64_t total = 0;
+  for (uint32_t q = 0; q < n; ++q) total += job->cycles[q];
+  res->device_ms = ms;
+  res->stream_cycles = total;
+  res->launches = 1;
+  if (res->final_reg_digest) TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outReg.p, n * 8ull, cudaMemcpyDeviceToHost, st));
+  if (res->final_mem_digest) TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outMem.p, n * 8ull, cudaMemcpyDeviceToHost, st));
+  if (res->rolling_digest) TGS_CUDA(cudaMemcpyAsync(res->rolling_digest, h->outRoll.p, n * 8ull, cudaMemcpyDeviceToHost, st));
+  if (res->stop_cycle) TGS_CUDA(cudaMemcpyAsync(res->stop_cycle, h->outStop.p, n * 4ull, cudaMemcpyDeviceToHost, st));
+  if (perCycle)
+    TGS_CUDA(cudaMemcpyAsync(res->cycle_digest, h->cycDig.p, size_t(n) * res->cycle_stride * 8, cudaMemcpyDeviceToHost, st));
+  TGS_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace
+
+// Streams of a job run from the initial state (or, with TGS_BATCH_CONTINUE,
+// from the previous call's state and cycle) for cycles[s] cycles each.
+void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
+  if (!job || !job->cycles || job->n_streams == 0) throw Error(TGS_ERR_ARG, "empty batch");
+  const uint32_t n = job->n_streams;
+  const tgs_stimulus *st = job->stim;
+  uint32_t flags = 0;
+  if (st && st->n_inputs) {
+    flags |= kFlagStimulus;
+    checkStimulus(h, st);
+  }
+  const bool wantDigest = (job->flags & (TGS_BATCH_CYCLE_DIGESTS | TGS_BATCH_ROLLING)) != 0;
+  if (wantDigest) flags |= kFlagDigest;
+  if (flags) checkRegionRoles(h);
+  if (flags & kFlagStimulus) {
+    h->stimReg.upload(st->reg, st->n_inputs, h->stream);
+    h->stimBits.upload(st->bits, st->n_inputs, h->stream);
+    if (st->toggle) h->stimToggle.upload(st->toggle, st->n_inputs, h->stream);
+  }
+  bool equal = true;
+  for (uint32_t s = 1; s < n; ++s) equal &= job->cycles[s] == job->cycles[0];
+  const bool admission = !equal || (job->slots && job->slots < n);
+  if (admission) {
+    if (job->flags & TGS_BATCH_CONTINUE) throw Error(TGS_ERR_ARG, "TGS_BATCH_CONTINUE needs every stream resident");
+    fillParams(h);  // refreshed below after any reconfiguration
+    batchAdmission(h, job, res, flags);
+    return;
+  }
+  const uint32_t cyc = job->cycles[0];
+  const bool cont = (job->flags & TGS_BATCH_CONTINUE) != 0;
+  if (cont && h->opt.n_streams != n) throw Error(TGS_ERR_STATE, "TGS_BATCH_CONTINUE with a different stream count");
+  if (h->opt.n_streams != n) {
+    h->opt.n_streams = n;
+    configure(h);
+  }
+  if (!cont) {
+    resetState(h);
+    h->batchCycle = 0;
+    TGS_CUDA(cudaMemsetAsync(h->roll.p, 0, n * 8ull, h->stream));
+  }
+  fillParams(h);
+  KParams &p = h->kp;
+  const uint32_t c0 = uint32_t(h->batchCycle);
+  if (flags & kFlagStimulus) {
+    p.nStim = st->n_inputs;
+    p.stimReg = h->stimReg.p;
+    p.stimBits = h->stimBits.p;
+    p.stimToggle = st->toggle ? h->stimToggle.p : nullptr;
+    std::vector<unsigned long long> seeds(n);
+    for (uint32_t s = 0; s < n; ++s) seeds[s] = mix64(st->base_seed ^ s);
+    h->seeds.upload(seeds, h->stream);
+    p.streamSeed = h->seeds.p;
+    if (st->table) {
+      h->stimTable.upload(st->table, size_t(cyc) * st->n_inputs * n, h->stream);
+      p.stimTable = h->stimTable.p;
+      p.stimTableC0 = c0;
+    }
+  }
+  TGS_CUDA(cudaMemsetAsync(h->digAcc.p, 0, n * 8ull, h->stream));
+  const bool perCycle = (job->flags & TGS_BATCH_CYCLE_DIGESTS) && res && res->cycle_digest && res->cycle_stride;
+  if (perCycle) {
+    h->cycDig.alloc(size_t(n) * res->cycle_stride);
+    TGS_CUDA(cudaMemsetAsync(h->cycDig.p, 0, size_t(n) * res->cycle_stride * 8, h->stream));
+    p.cycDig = h->cycDig.p;
+    p.cycStride = res->cycle_stride;
+    p.cycBase = c0;
+  }
+  const float ms = runTimed(h, c0, cyc, flags);
+  h->batchCycle += cyc;
+  h->cycleCnt = h->batchCycle;
   if (!res) return;
   res->device_ms = ms;
   res->stream_cycles = uint64_t(cyc) * n;
   res->launches = 1;
+  cudaStream_t s = h->stream;
   if (res->final_reg_digest || res->final_mem_digest) {
-    TGS_CUDA(cudaMemsetAsync(h->outA.p, 0, n * 8, h->stream));
-    TGS_CUDA(cudaMemsetAsync(h->outB.p, 0, n * 8, h->stream));
-    TGS_CUDA(launchRegDigest(int(h->spw), h->regs.p, h->design.regPoolSize, h->gpad, n, h->outA.p, h->stream));
-    TGS_CUDA(launchMemDigest(h->mems.p, h->memStride, h->design.memPoolSize, n, h->outB.p, h->stream));
-    if (res->final_reg_digest) TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outA.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
-    if (res->final_mem_digest) TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outB.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaMemsetAsync(h->outA.p, 0, n * 8ull, s));
+    TGS_CUDA(cudaMemsetAsync(h->outB.p, 0, n * 8ull, s));
+    if (res->final_reg_digest) {
+      TGS_CUDA(launchRegDigest(int(h->spw), h->regs.p, h->design.regPoolSize, h->gpad, n, h->outA.p, s));
+      TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outA.p, n * 8ull, cudaMemcpyDeviceToHost, s));
+    }
+    if (res->final_mem_digest) {
+      TGS_CUDA(launchMemDigest(h->mems.p, h->memStride, h->design.memPoolSize, n, h->outB.p, s));
+      TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outB.p, n * 8ull, cudaMemcpyDeviceToHost, s));
+    }
   }
-  if (res->rolling_digest) TGS_CUDA(cudaMemcpyAsync(res->rolling_digest, h->roll.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (res->rolling_digest) TGS_CUDA(cudaMemcpyAsync(res->rolling_digest, h->roll.p, n * 8ull, cudaMemcpyDeviceToHost, s));
   if (perCycle)
-    TGS_CUDA(cudaMemcpyAsync(res->cycle_digest, h->cycDig.p, size_t(n) * res->cycle_stride * 8, cudaMemcpyDeviceToHost, h->stream));
-  if (res->stop_cycle) TGS_CUDA(cudaMemcpyAsync(res->stop_cycle, h->stopCycle.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
-  TGS_CUDA(cudaStreamSynchronize(h->stream));
+    TGS_CUDA(cudaMemcpyAsync(res->cycle_digest, h->cycDig.p, size_t(n) * res->cycle_stride * 8, cudaMemcpyDeviceToHost, s));
+  if (res->stop_cycle) TGS_CUDA(cudaMemcpyAsync(res->stop_cycle, h->stopCycle.p, n * 4ull, cudaMemcpyDeviceToHost, s));
+  TGS_CUDA(cudaStreamSynchronize(s));
   if (res->final_regs || res->final_mems) {
-    std::vector<uint8_t> buf;
-    for (uint32_t s = 0; s < n; ++s) {
-      uint32_t g = s / h->spw, k = s % h->spw;
+    for (uint32_t q = 0; q < n; ++q) {
+      uint32_t g = q / h->spw, k = q % h->spw;
       if (res->final_regs) {
         h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
-        TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
-        TGS_CUDA(cudaMemcpyAsync(res->final_regs + size_t(s) * h->design.regPoolSize, h->ioBytes.p,
-                                 h->design.regPoolSize, cudaMemcpyDeviceToHost, h->stream));
-        TGS_CUDA(cudaStreamSynchronize(h->stream));
+        TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, s));
+        TGS_CUDA(cudaMemcpyAsync(res->final_regs + size_t(q) * h->design.regPoolSize, h->ioBytes.p,
+                                 h->design.regPoolSize, cudaMemcpyDeviceToHost, s));
+        TGS_CUDA(cudaStreamSynchronize(s));
       }
       if (res->final_mems)
-        TGS_CUDA(cudaMemcpy(res->final_mems + size_t(s) * h->design.memPoolSize, h->mems.p + size_t(s) * h->memStride,
+        TGS_CUDA(cudaMemcpy(res->final_mems + size_t(q) * h->design.memPoolSize, h->mems.p + size_t(q) * h->memStride,
                             h->design.memPoolSize, cudaMemcpyDeviceToHost));
     }
   }
@@ -984,5 +1168,18 @@ extern "C" int tgs_initial_state(const char *design_path, const char *symbol_pat
       throw Error(TGS_ERR_ARG, "buffers must hold regPoolSize and memPoolSize bytes");
     if (regs && reg_bytes) std::memcpy(regs, d.regPool.data(), reg_bytes);
     if (mems && mem_bytes) std::memcpy(mems, d.memPool.data(), mem_bytes);
+  });
+}
+
+extern "C" int tgs_host_alloc(size_t bytes, void **out) {
+  return guard([&] {
+    if (!out) throw Error(TGS_ERR_ARG, "null output");
+    TGS_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+  });
+}
+
+extern "C" int tgs_host_free(void *p) {
+  return guard([&] {
+    if (p) TGS_CUDA(cudaFreeHost(p));
   });
 }

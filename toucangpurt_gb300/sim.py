@@ -168,7 +168,8 @@ class Simulator:
 
     # -- batched runs ---------------------------------------------------------
     def batch_run(self, cycles, stim: "StimulusSpec | None" = None, *, cycle_digests: bool = False,
-                  rolling: bool = True, final_state: bool = False, slots: int = 0) -> "BatchOutput":
+                  rolling: bool = True, final_state: bool = False, slots: int = 0, continue_: bool = False,
+                  final_digests: bool = True) -> "BatchOutput":
         cyc = np.ascontiguousarray(cycles, np.uint32)
         n = int(cyc.size)
         out = BatchOutput(n)
@@ -180,7 +181,7 @@ class Simulator:
             out.final_regs = np.zeros((n, r), np.uint8)
             out.final_mems = np.zeros((n, m), np.uint8)
         flags = (capi.BATCH_CYCLE_DIGESTS if cycle_digests else 0) | (capi.BATCH_ROLLING if rolling else 0) | (
-            capi.BATCH_FINAL_STATE if final_state else 0)
+            capi.BATCH_FINAL_STATE if final_state else 0) | (capi.BATCH_CONTINUE if continue_ else 0)
         st_ptr = C.cast(None, C.POINTER(capi.Stimulus))
         keep = []
         if stim is not None:
@@ -189,8 +190,8 @@ class Simulator:
             st_ptr = C.pointer(s[0])
         job = capi.Batch(n, _ptr(cyc, C.c_uint32), st_ptr, flags, slots)
         res = capi.BatchResult()
-        res.final_reg_digest = _ptr(out.final_reg_digest, C.c_uint64)
-        res.final_mem_digest = _ptr(out.final_mem_digest, C.c_uint64)
+        res.final_reg_digest = _ptr(out.final_reg_digest if final_digests else None, C.c_uint64)
+        res.final_mem_digest = _ptr(out.final_mem_digest if final_digests else None, C.c_uint64)
         res.rolling_digest = _ptr(out.rolling_digest, C.c_uint64)
         res.cycle_digest = _ptr(out.cycle_digest, C.c_uint64)
         res.cycle_stride = stride
@@ -212,13 +213,18 @@ class StimulusSpec:
     reg: np.ndarray
     bits: np.ndarray
     toggle: np.ndarray | None = None
+    table: np.ndarray | None = None  # [cycle][input][stream] nibbles (replaces the seeded values)
 
     def to_c(self):
         reg = np.ascontiguousarray(self.reg, np.uint32)
         bits = np.ascontiguousarray(self.bits, np.uint8)
         tog = None if self.toggle is None else np.ascontiguousarray(self.toggle, np.uint16)
-        s = capi.Stimulus(self.base_seed, reg.size, _ptr(reg, C.c_uint32), _ptr(bits, C.c_uint8), _ptr(tog, C.c_uint16))
-        return (s, reg, bits, tog)
+        tab = None if self.table is None else self.table
+        if tab is not None and not (tab.flags.c_contiguous and tab.dtype == np.uint8):
+            raise ValueError("stimulus table must be a C-contiguous uint8 array")
+        s = capi.Stimulus(self.base_seed, reg.size, _ptr(reg, C.c_uint32), _ptr(bits, C.c_uint8), _ptr(tog, C.c_uint16),
+                          _ptr(tab, C.c_uint8))
+        return (s, reg, bits, tog, tab)
 
 
 @dataclass
@@ -272,3 +278,58 @@ def validate_file(design_path, symbol_path=None) -> int:
     sym = str(symbol_path).encode() if symbol_path else None
     check(lib().tgs_validate_file(str(design_path).encode(), sym, C.byref(n)))
     return n.value
+
+
+# ---- seeded stimulus on the host ------------------------------------------------
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def mix64(z: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser (Steele, Lea, Flood), vectorised over uint64."""
+    with np.errstate(over="ignore"):
+        z = (z + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return z ^ (z >> np.uint64(31))
+
+
+def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out: np.ndarray | None = None) -> np.ndarray:
+    """The seeded input values of cycles [c0, c0 + cycles) as a host table
+    [cycle][input][stream] (uniform inputs only), identical to what the
+    device computes from the seed."""
+    if spec.toggle is not None and np.any(spec.toggle):
+        raise ValueError("toggle inputs depend on the previous value; tables hold uniform inputs")
+    n_in = len(spec.reg)
+    seeds = mix64(np.uint64(spec.base_seed) ^ np.arange(n_streams, dtype=np.uint64))
+    masks = ((np.uint32(1) << np.asarray(spec.bits, np.uint32)) - 1).astype(np.uint64)
+    if out is None:
+        out = np.empty((cycles, n_in, n_streams), np.uint8)
+    inp = np.arange(n_in, dtype=np.uint64)
+    for c in range(cycles):
+        key = mix64((np.uint64(c0 + c) << np.uint64(32)) | inp)           # [n_in]
+        h = mix64(seeds[None, :] ^ key[:, None])                          # [n_in, n_streams]
+        out[c] = (h & masks[:, None]).astype(np.uint8)
+    return out
+
+
+class PinnedBuffer:
+    """Page-locked host buffer from tgs_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, shape, dtype=np.uint8):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = C.c_void_p()
+        check(lib().tgs_host_alloc(n, C.byref(self._p)))
+        buf = (C.c_uint8 * n).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().tgs_host_free(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
