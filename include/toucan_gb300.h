@@ -227,6 +227,46 @@ typedef struct tgs_design_stats {
 } tgs_design_stats;
 int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *out);
 
+/* ---- learned cost model of micro-partitions (new) ----------------------- */
+/* The scheduler (options.schedule = TGS_SCHED_LEARNED) balances warps and
+ * blocks on a cost predicted by a 16-64-64-1 FP32 MLP from 16 structural
+ * features of each micro-partition, trained with Adam on clock64 timings the
+ * cycle kernel records; gate count (TGS_SCHED_GREEDY) is the fallback.
+ * Values never depend on the schedule. */
+typedef struct tgs_train_opts {
+  uint32_t epochs;   /* default 30 */
+  uint32_t batch;    /* default 1024 */
+  float lr;          /* default 2e-3 */
+  uint64_t seed;
+  float val_frac;    /* held-out fraction for the report (<= 0.5) */
+  uint32_t reserved[4];
+} tgs_train_opts;
+
+typedef struct tgs_train_report {
+  float train_mse, val_mse;  /* standardised log-cycle space */
+  float val_corr;            /* correlation of predicted and measured log cycles (held out) */
+  float gate_corr;           /* same for log gate count (the greedy cost) */
+  uint32_t samples, epochs;
+  double train_ms;
+  uint32_t reserved[4];
+} tgs_train_report;
+
+int tgs_num_mparts(tgs_sim *h, uint32_t *n);
+/* features[id * 16 + f] of every micro-partition (id = design order) */
+int tgs_mpart_features(tgs_sim *h, float *features, uint32_t n);
+/* runs `cycles` cycles of every stream with per-micro-partition clock64
+ * timing; mean_cycles[id] = mean cycles of one evaluation */
+int tgs_profile_mparts(tgs_sim *h, uint32_t cycles, float *mean_cycles, uint32_t n);
+/* trains the handle's cost model (rebuilds a learned schedule) */
+int tgs_cost_model_train(tgs_sim *h, const float *features, const float *cycles, uint32_t n, const tgs_train_opts *opts,
+                         tgs_train_report *report);
+/* get (set = 0) or set (set = 1) the 5,313 parameters + (mean, std) of log cycles */
+int tgs_cost_model_state(tgs_sim *h, float *state, size_t n, int set);
+/* the network's kernels on host buffers: outputs for n feature rows, and the
+ * mean-squared-error gradient (for checks against a CPU reference) */
+int tgs_mlp_forward(const float *params, const float *X, uint32_t n, float *out);
+int tgs_mlp_grad(const float *params, const float *X, const float *y, uint32_t n, float *grad, float *loss);
+
 /* ---- synthetic designs (new; the reference ships no design or compiler) */
 typedef struct tgs_gen_config {
   uint64_t seed;

@@ -100,6 +100,18 @@ class DesignStats(C.Structure):
     ]
 
 
+class TrainOpts(C.Structure):
+    _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64),
+                ("val_frac", C.c_float), ("reserved", C.c_uint32 * 4)]
+
+
+class TrainReport(C.Structure):
+    _fields_ = [("train_mse", C.c_float), ("val_mse", C.c_float), ("val_corr", C.c_float), ("gate_corr", C.c_float),
+                ("samples", C.c_uint32), ("epochs", C.c_uint32), ("train_ms", C.c_double), ("reserved", C.c_uint32 * 4)]
+
+
+MLP_PARAMS = 5313
+
 # (name, argtypes) of every exported entry point; all return int status
 # except tgs_last_error / tgs_version.
 SIGNATURES = {
@@ -134,6 +146,15 @@ SIGNATURES = {
     "tgs_get_design_stats": [C.c_void_p, C.POINTER(DesignStats)],
     "tgs_host_alloc": [C.c_size_t, C.POINTER(C.c_void_p)],
     "tgs_host_free": [C.c_void_p],
+    "tgs_num_mparts": [C.c_void_p, u32p],
+    "tgs_mpart_features": [C.c_void_p, C.POINTER(C.c_float), C.c_uint32],
+    "tgs_profile_mparts": [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_uint32],
+    "tgs_cost_model_train": [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32,
+                             C.POINTER(TrainOpts), C.POINTER(TrainReport)],
+    "tgs_cost_model_state": [C.c_void_p, C.POINTER(C.c_float), C.c_size_t, C.c_int],
+    "tgs_mlp_forward": [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float)],
+    "tgs_mlp_grad": [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32,
+                     C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "tgs_default_gen_config": [C.POINTER(GenConfig)],
     "tgs_generate": [C.POINTER(GenConfig), C.c_char_p, C.c_char_p, C.POINTER(GenInfo)],
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],

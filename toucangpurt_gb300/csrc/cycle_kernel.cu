@@ -409,9 +409,11 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     }
     const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
     const uint32_t *units = blk + 2 + NW;
+    const bool profileMP = (p.flags & kFlagProfileMP) != 0;
     for (uint32_t u = ub; u < ue; ++u) {
       const uint32_t *mp = blk + units[u];
       const uint32_t hdr = mp[0];
+      const long long tm = profileMP ? clock64() : 0;
       switch (hdr & 3u) {
         case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;
         case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane); break;
@@ -419,6 +421,11 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
         default: evalMemRead<SPW, G>(p, mp, hdr, vp, lane, gb); break;
       }
       __syncwarp();
+      if (profileMP && lane == 0) {
+        const uint32_t id = mp[1];
+        atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
+        atomicAdd(p.mpCount + id, 1u);
+      }
     }
   }
   __syncthreads();

@@ -128,6 +128,9 @@ struct KParams {
   unsigned long long *outReg, *outMem, *outRoll;  // [jobs]
   uint32_t *outStop;          // [jobs]
   uint32_t nEvents, nJobs;
+  // per-micro-partition clock64 profile (kFlagProfileMP), indexed by the id in header word 1
+  unsigned long long *mpCycles;
+  uint32_t *mpCount;
 };
 
 constexpr uint32_t kNoStream = 0xFFFFFFFFu;
@@ -137,7 +140,8 @@ enum : uint32_t {
   kFlagDigest = 2u,     // per-cycle register digests (rolling / per-cycle array)
   kFlagProfile = 4u,    // per-partition clock64 profile (free-running)
   kFlagCountCycles = 8u, // advance realCycles (free-running launches only, SimEval.cu:985-989)
-  kFlagSlots = 16u       // job streams queued onto resident slots, retired and admitted in place
+  kFlagSlots = 16u,      // job streams queued onto resident slots, retired and admitted in place
+  kFlagProfileMP = 32u   // clock64 cycles of every micro-partition evaluation (cost-model samples)
 };
 
 enum : uint32_t {

@@ -206,11 +206,35 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img) {
         ref.feat.partLevels = pd.nLevels;
         ref.off = m.isLUTPart ? emitLut(m, net, ref.feat) : emitSpecial(m, net, ref.feat);
         ref.words = uint32_t((net.size() + 3) / 4 * 4) - ref.off;
+        ref.id = img.nMParts++;
+        net[ref.off + 1] = ref.id;  // header word 1: design-wide micro-partition id (profiling)
         accessOf(m, ref.reads, ref.writes);
         std::sort(ref.reads.begin(), ref.reads.end());
         ref.reads.erase(std::unique(ref.reads.begin(), ref.reads.end()), ref.reads.end());
         ref.feat.fanIn = uint32_t(ref.reads.size());
         img.mp[pid][lv].push_back(std::move(ref));
+      }
+    }
+    // fan-out: later reads of each micro-partition's outputs within the partition
+    {
+      std::vector<int64_t> writer(std::max<uint32_t>(p.valuePoolSize, 16) + 64, -1);
+      std::vector<MPartRef *> flat;
+      for (auto &lvl : img.mp[pid])
+        for (auto &r : lvl) flat.push_back(&r);
+      size_t idx = 0;
+      for (auto &lvl : img.mp[pid]) {
+        const size_t first = idx;
+        for (auto &r : lvl) {
+          for (uint32_t sl : r.reads)
+            if (sl < writer.size() && writer[sl] >= 0) flat[size_t(writer[sl])]->feat.fanOut++;
+          ++idx;
+        }
+        idx = first;
+        for (auto &r : lvl) {
+          for (uint32_t sl : r.writes)
+            if (sl < writer.size()) writer[sl] = int64_t(idx);
+          ++idx;
+        }
       }
     }
     // last level

@@ -29,6 +29,7 @@ struct MPartFeat {
 struct MPartRef {
   uint32_t off = 0;    // word offset in DeviceImage::net
   uint32_t words = 0;  // record size, multiple of 4
+  uint32_t id = 0;     // design-wide micro-partition index
   MPartFeat feat;
   std::vector<uint32_t> reads, writes;
 };
@@ -40,6 +41,7 @@ struct DeviceImage {
   std::vector<uint32_t> partRegion;
   std::vector<std::vector<std::vector<MPartRef>>> mp;  // [part][level][i]
   uint32_t maxVpSlots = 0;
+  uint32_t nMParts = 0;
 };
 
 struct Schedule {

@@ -107,6 +107,8 @@ struct tgs_sim {
       outStop;
   tgs::DBuf<unsigned long long> jobSeed, memAcc, outReg, outMem, outRoll;
   tgs::DBuf<uint8_t> stimTable;
+  tgs::DBuf<unsigned long long> mpCycles;
+  tgs::DBuf<uint32_t> mpCount;
   uint64_t batchCycle = 0;  // cycles run by TGS_BATCH_CONTINUE batches since the last reset
   tgs::DBuf<uint8_t> ioBytes;
   tgs::KParams kp{};
@@ -1181,5 +1183,137 @@ extern "C" int tgs_host_alloc(size_t bytes, void **out) {
 extern "C" int tgs_host_free(void *p) {
   return guard([&] {
     if (p) TGS_CUDA(cudaFreeHost(p));
+  });
+}
+
+// ---- learned cost model ---------------------------------------------------------
+namespace {
+void requireModel(tgs_sim *h) {
+  if (!h->model) h->model = std::make_unique<tgs::CostModel>();
+}
+}  // namespace
+
+extern "C" int tgs_num_mparts(tgs_sim *h, uint32_t *n) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!n) throw Error(TGS_ERR_ARG, "null output");
+    *n = h->img.nMParts;
+  });
+}
+
+extern "C" int tgs_mpart_features(tgs_sim *h, float *features, uint32_t n) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!features || n != h->img.nMParts) throw Error(TGS_ERR_ARG, "features must hold n_mparts x 16 floats");
+    for (auto &p : h->img.mp)
+      for (auto &l : p)
+        for (auto &r : l) featureVector(r.feat, features + size_t(r.id) * kFeatures);
+  });
+}
+
+extern "C" int tgs_profile_mparts(tgs_sim *h, uint32_t cycles, float *mean_cycles, uint32_t n) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!mean_cycles || n != h->img.nMParts) throw Error(TGS_ERR_ARG, "mean_cycles must hold n_mparts floats");
+    h->mpCycles.alloc(n);
+    h->mpCount.alloc(n);
+    TGS_CUDA(cudaMemsetAsync(h->mpCycles.p, 0, size_t(n) * 8, h->stream));
+    TGS_CUDA(cudaMemsetAsync(h->mpCount.p, 0, size_t(n) * 4, h->stream));
+    fillParams(h);
+    h->kp.mpCycles = h->mpCycles.p;
+    h->kp.mpCount = h->mpCount.p;
+    runCycles(h, uint32_t(h->cycleCnt), cycles, kFlagProfileMP);
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    checkDeviceError(h);
+    h->cycleCnt += cycles;
+    std::vector<unsigned long long> c(n);
+    std::vector<uint32_t> k(n);
+    TGS_CUDA(cudaMemcpy(c.data(), h->mpCycles.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
+    TGS_CUDA(cudaMemcpy(k.data(), h->mpCount.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < n; ++i) mean_cycles[i] = k[i] ? float(double(c[i]) / k[i]) : 0.f;
+    fillParams(h);
+  });
+}
+
+extern "C" int tgs_cost_model_train(tgs_sim *h, const float *features, const float *cycles, uint32_t n,
+                                    const tgs_train_opts *o, tgs_train_report *rep) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!features || !cycles) throw Error(TGS_ERR_ARG, "null argument");
+    requireModel(h);
+    tgs_train_opts d{};
+    d.epochs = 30;
+    d.batch = 1024;
+    d.lr = 2e-3f;
+    d.seed = 1;
+    d.val_frac = 0.2f;
+    const tgs_train_opts &t = o ? *o : d;
+    auto r = h->model->train(features, cycles, n, t.epochs ? t.epochs : d.epochs, t.batch ? t.batch : d.batch,
+                             t.lr > 0 ? t.lr : d.lr, t.seed, t.val_frac);
+    if (rep) {
+      std::memset(rep, 0, sizeof(*rep));
+      rep->train_mse = r.trainMse;
+      rep->val_mse = r.valMse;
+      rep->val_corr = r.valCorr;
+      rep->gate_corr = r.gateCorr;
+      rep->samples = r.samples;
+      rep->epochs = r.epochs;
+      rep->train_ms = r.ms;
+    }
+    if (h->opt.schedule == TGS_SCHED_LEARNED) {
+      configure(h);
+      resetState(h);
+    }
+  });
+}
+
+extern "C" int tgs_cost_model_state(tgs_sim *h, float *state, size_t n, int set) {
+  return guard([&] {
+    if (!h || !state) throw Error(TGS_ERR_ARG, "null argument");
+    if (n != size_t(kMlpParams) + 2) throw Error(TGS_ERR_ARG, "cost model state holds 5,315 floats");
+    requireModel(h);
+    if (set) {
+      h->model->setState(std::vector<float>(state, state + n));
+      if (h->loaded && h->opt.schedule == TGS_SCHED_LEARNED) {
+        TGS_CUDA(cudaSetDevice(h->device));
+        configure(h);
+        resetState(h);
+      }
+    } else {
+      if (!h->model->trained()) throw Error(TGS_ERR_STATE, "cost model not trained");
+      auto s = h->model->state();
+      std::memcpy(state, s.data(), n * sizeof(float));
+    }
+  });
+}
+
+extern "C" int tgs_mlp_forward(const float *params, const float *X, uint32_t n, float *out) {
+  return guard([&] {
+    if (!params || !X || !out) throw Error(TGS_ERR_ARG, "null argument");
+    DBuf<float> dp, dx, dy;
+    dp.upload(params, kMlpParams, nullptr);
+    dx.upload(X, size_t(n) * kFeatures, nullptr);
+    dy.alloc(n);
+    TGS_CUDA(mlpForward(dp.p, dx.p, n, dy.p, nullptr));
+    TGS_CUDA(cudaMemcpy(out, dy.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
+  });
+}
+
+extern "C" int tgs_mlp_grad(const float *params, const float *X, const float *y, uint32_t n, float *grad, float *loss) {
+  return guard([&] {
+    if (!params || !X || !y || !grad) throw Error(TGS_ERR_ARG, "null argument");
+    DBuf<float> dp, dx, dy, dg, dl;
+    dp.upload(params, kMlpParams, nullptr);
+    dx.upload(X, size_t(n) * kFeatures, nullptr);
+    dy.upload(y, n, nullptr);
+    dg.alloc(kMlpParams);
+    dl.alloc(1);
+    TGS_CUDA(cudaMemset(dg.p, 0, kMlpParams * 4));
+    TGS_CUDA(cudaMemset(dl.p, 0, 4));
+    TGS_CUDA(mlpGrad(dp.p, dx.p, dy.p, nullptr, n, n ? 1.f / float(n) : 0.f, dg.p, dl.p, nullptr));
+    TGS_CUDA(cudaMemcpy(grad, dg.p, kMlpParams * 4, cudaMemcpyDeviceToHost));
+    float l = 0;
+    TGS_CUDA(cudaMemcpy(&l, dl.p, 4, cudaMemcpyDeviceToHost));
+    if (loss) *loss = n ? l / float(n) : 0.f;
   });
 }

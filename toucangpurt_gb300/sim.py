@@ -333,3 +333,68 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+# ---- learned cost model ------------------------------------------------------------
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def mlp_forward(params: np.ndarray, X: np.ndarray) -> np.ndarray:
+    """The cost model's forward kernel on host arrays (standardised output)."""
+    p, x = _f32(params), _f32(X)
+    out = np.zeros(x.shape[0], np.float32)
+    check(lib().tgs_mlp_forward(_ptr(p, C.c_float), _ptr(x, C.c_float), x.shape[0], _ptr(out, C.c_float)))
+    return out
+
+
+def mlp_grad(params: np.ndarray, X: np.ndarray, y: np.ndarray) -> tuple[np.ndarray, float]:
+    """Gradient of the mean squared error computed by the backward kernel."""
+    p, x, t = _f32(params), _f32(X), _f32(y)
+    g = np.zeros(capi.MLP_PARAMS, np.float32)
+    loss = C.c_float()
+    check(lib().tgs_mlp_grad(_ptr(p, C.c_float), _ptr(x, C.c_float), _ptr(t, C.c_float), x.shape[0],
+                             _ptr(g, C.c_float), C.byref(loss)))
+    return g, loss.value
+
+
+def _sim_learned_methods():
+    def n_mparts(self) -> int:
+        n = C.c_uint32()
+        check(lib().tgs_num_mparts(self._h, C.byref(n)))
+        return n.value
+
+    def mpart_features(self) -> np.ndarray:
+        n = self.n_mparts()
+        x = np.zeros((n, 16), np.float32)
+        check(lib().tgs_mpart_features(self._h, _ptr(x, C.c_float), n))
+        return x
+
+    def profile_mparts(self, cycles: int) -> np.ndarray:
+        n = self.n_mparts()
+        c = np.zeros(n, np.float32)
+        check(lib().tgs_profile_mparts(self._h, int(cycles), _ptr(c, C.c_float), n))
+        return c
+
+    def train_cost_model(self, features, cycles, *, epochs=30, batch=1024, lr=2e-3, seed=1, val_frac=0.2) -> dict:
+        x, c = _f32(features), _f32(cycles)
+        o = capi.TrainOpts(epochs, batch, lr, seed, val_frac)
+        r = capi.TrainReport()
+        check(lib().tgs_cost_model_train(self._h, _ptr(x, C.c_float), _ptr(c, C.c_float), x.shape[0], C.byref(o),
+                                         C.byref(r)))
+        return {f: getattr(r, f) for f, _ in capi.TrainReport._fields_ if f != "reserved"}
+
+    def cost_model_state(self) -> np.ndarray:
+        s = np.zeros(capi.MLP_PARAMS + 2, np.float32)
+        check(lib().tgs_cost_model_state(self._h, _ptr(s, C.c_float), s.size, 0))
+        return s
+
+    def set_cost_model_state(self, state) -> None:
+        s = _f32(state)
+        check(lib().tgs_cost_model_state(self._h, _ptr(s, C.c_float), s.size, 1))
+
+    for f in (n_mparts, mpart_features, profile_mparts, train_cost_model, cost_model_state, set_cost_model_state):
+        setattr(Simulator, f.__name__, f)
+
+
+_sim_learned_methods()
