@@ -48,6 +48,9 @@ def args_parse():
     p.add_argument("--warps", type=int, default=8)
     p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
     p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
+    p.add_argument("--autotune", action="store_true", help="time the launch configurations first and keep the fastest")
+    p.add_argument("--mode", default="persistent", choices=["persistent", "graph"],
+                   help="cycle loop as one persistent launch or as replayed CUDA-graph chunks (one launch per region)")
     p.add_argument("--slots", type=int, default=0, help="resident slots for queued streams of uneven length")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cycles", type=int, default=1)
@@ -257,13 +260,30 @@ def run_reference_gpu(a, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def prepare(a, s):
+    """Learned schedule (profile micro-partitions, train the cost model) and
+    autotuning, both before the timed region.  Returns notes for `config`."""
+    notes = {}
+    if a.schedule == "learned":
+        rep = s.train_cost_model(s.mpart_features(), s.profile_mparts(20), epochs=40, seed=5)
+        s.set_options(schedule=1)
+        notes["cost_model"] = {k: round(float(v), 4) for k, v in rep.items() if k in ("val_mse", "val_corr", "gate_corr")}
+    if a.autotune:
+        best, trials = s.autotune(cycles=8, warmup=2)
+        notes["autotuned"] = {k: best[k] for k in ("groups_per_item", "warps_per_block", "blocks_per_sm", "mode", "staged")}
+        notes["autotune_trials"] = len(trials)
+    return notes
+
+
 def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     """Streams of log-uniform length queued onto resident slots (retired and
     admitted in place inside one persistent launch).  One step = the whole job."""
     from toucangpurt_gb300 import sim, workloads
 
-    s = sim.Simulator(n_streams=8, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule)
+    s = sim.Simulator(n_streams=a.slots or 1024, groups_per_item=a.groups, warps_per_block=a.warps,
+                      mode=1 if a.mode == "graph" else 0)
     s.init(gpu, dp, sp, False, False)
+    notes = prepare(a, s)
     cyc = workloads.stream_lengths(a.workload, streams, seed=7 + rank)
     stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], workloads.toggles(a.workload, info["pi_bits"]))
     for _ in range(a.warmup):
@@ -271,9 +291,11 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     barrier(ws)
     clk = Clocks(gpu)
     dev_ms, t0 = 0.0, time.perf_counter()
+    launches = 0
     for _ in range(a.steps):
         out = s.batch_run(cyc, stim, rolling=False, slots=a.slots)
         dev_ms += out.device_ms
+        launches += out.launches
     wall = time.perf_counter() - t0
     clocks = clk.stop()
     st = s.design_stats()
@@ -288,11 +310,11 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
                                    f"(mean {cyc.mean():.0f}), {st['streams_per_word'] * 0 + (a.slots or min(streams, 1024))} slots",
                        "stream_cycles": int(cyc.sum()), "blocks": st["blocks"], "threads_per_block": st["threads"],
-                       "groups_per_item": st["groups_per_item"]},
+                       "groups_per_item": st["groups_per_item"], **notes},
             "lut_evals_per_s": total / dev_s * st["lut_ops"],
             "e2e": {"value": total / wall_s, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": int(cyc.nbytes),
                     "d2h_bytes_per_step": int(streams * 8 * 3)},
-            "gpu_launches": a.steps, "clocks": clocks,
+            "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     s.cleanup()
@@ -310,9 +332,10 @@ def run_gb300(a, rank, ws):
     schedule = 1 if a.schedule == "learned" else 0
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
         return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
-    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps, schedule=schedule,
-                      resident_netlist=2 if a.no_stage else 0)
+    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps,
+                      resident_netlist=2 if a.no_stage else 0, mode=1 if a.mode == "graph" else 0)
     s.init(gpu, dp, sp, False, False)
+    notes = prepare(a, s)
     st = s.design_stats()
     toggle = workloads.toggles(a.workload, info["pi_bits"])
     stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], toggle)
@@ -352,6 +375,7 @@ def run_gb300(a, rank, ws):
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams, {cps} cycles per step",
                        "streams": streams, "cycles_per_step": cps, "lut_ops": st["lut_ops"],
                        "partitions": st["partitions"], "schedule": a.schedule, "groups_per_item": st["groups_per_item"],
+                       "mode": ["persistent", "graph"][s.options()["mode"]], **notes,
                        "threads_per_block": st["threads"], "blocks": st["blocks"],
                        "l2": "working set (memories) larger than L2"},
             "lut_evals_per_s": value * st["lut_ops"],

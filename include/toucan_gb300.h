@@ -76,6 +76,29 @@ typedef struct tgs_options {
 #define TGS_MODE_GRAPH 1u
 
 int tgs_default_options(tgs_options *opt);
+
+/* Autotuner (no counterpart in the reference): times short runs of the loaded
+ * design at the handle's stream count over groups_per_item x warps_per_block
+ * x blocks_per_sm x mode (x staging), keeps the fastest as the handle's
+ * options and resets the state to the initial state.  Micro-partition sizes
+ * are fixed by the design file; these are the launch-side knobs. */
+typedef struct tgs_tune_opts {
+  uint32_t cycles;       /* timed cycles per trial (0 = 16) */
+  uint32_t warmup;       /* untimed cycles per trial (0 = 2) */
+  uint32_t modes;        /* bit 0: persistent, bit 1: graph (0 = both) */
+  uint32_t try_unstaged; /* also try exec levels read from global memory */
+  uint32_t reserved[4];
+} tgs_tune_opts;
+
+typedef struct tgs_tune_trial {
+  uint32_t groups_per_item, warps_per_block, blocks_per_sm, mode, staged;
+  uint32_t blocks;      /* grid size of the trial */
+  float ms_per_cycle;   /* negative: the configuration does not fit */
+} tgs_tune_trial;
+
+/* trials (optional, max_trials entries) receives every trial; best receives the winner */
+int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, uint32_t max_trials,
+                 uint32_t *n_trials, tgs_tune_trial *best);
 /* Takes effect at the next tgs_init / tgs_init_from_memory; n_streams and the
  * schedule may also be changed after init (state is reset to the initial state). */
 int tgs_set_options(tgs_sim *h, const tgs_options *opt);

@@ -95,7 +95,7 @@ def test_table_and_continue_match_single_run(batch_design):
         for k in range(steps):
             sim.stimulus_table(spec, n, k * per, per, out=pinned.array)
             tspec = sim.StimulusSpec(11, info["pi_ids"], info["pi_bits"], table=pinned.array)
-            got = s.batch_run(np.full(n, per, np.uint32), tspec, continue_=True, final_digests=(k == steps - 1))
+            got = s.batch_run(np.full(n, per, np.uint32), tspec, continue_=k > 0, final_digests=(k == steps - 1))
         pinned.free()
     ref = pyoracle.OracleDesign(dp, sp).run(np.full(n, steps * per, np.uint32), spec)
     np.testing.assert_array_equal(one.final_reg_digest, ref["final_reg_digest"])

@@ -110,6 +110,16 @@ class TrainReport(C.Structure):
                 ("samples", C.c_uint32), ("epochs", C.c_uint32), ("train_ms", C.c_double), ("reserved", C.c_uint32 * 4)]
 
 
+class TuneOpts(C.Structure):
+    _fields_ = [("cycles", C.c_uint32), ("warmup", C.c_uint32), ("modes", C.c_uint32), ("try_unstaged", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
+
+
+class TuneTrial(C.Structure):
+    _fields_ = [("groups_per_item", C.c_uint32), ("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("mode", C.c_uint32), ("staged", C.c_uint32), ("blocks", C.c_uint32), ("ms_per_cycle", C.c_float)]
+
+
 MLP_PARAMS = 5313
 
 # (name, argtypes) of every exported entry point; all return int status
@@ -119,6 +129,8 @@ SIGNATURES = {
     "tgs_destroy": [C.c_void_p],
     "tgs_default_options": [C.POINTER(Options)],
     "tgs_set_options": [C.c_void_p, C.POINTER(Options)],
+    "tgs_autotune": [C.c_void_p, C.POINTER(TuneOpts), C.POINTER(TuneTrial), C.c_uint32, C.POINTER(C.c_uint32),
+                     C.POINTER(TuneTrial)],
     "tgs_get_options": [C.c_void_p, C.POINTER(Options)],
     "tgs_init": [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p, C.c_int, C.c_int],
     "tgs_init_from_memory": [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int, C.c_int],

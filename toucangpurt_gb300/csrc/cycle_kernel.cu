@@ -774,26 +774,71 @@ __device__ bool stageTable(const KParams &p, uint8_t *tab) {
 }
 
 // ---- kernels -----------------------------------------------------------------
+// Shared-memory layout of a block: truth table, two exec-level stage buffers,
+// value pool.  Returns false when staging the table timed out.
+struct BlockSmem {
+  uint8_t *tab;
+  uint32_t *vp;
+  Stage st;
+};
+
+__device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsigned long long *stageMbar, BlockSmem &b) {
+  b.tab = smem;
+  b.st.buf[0] = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
+  b.st.buf[1] = b.st.buf[0] + p.stageWords;
+  b.st.mb[0] = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
+  b.st.mb[1] = uint32_t(__cvta_generic_to_shared(&stageMbar[1]));
+  b.st.uses[0] = b.st.uses[1] = 0;
+  b.vp = b.st.buf[1] + p.stageWords;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb[0]) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb[1]) : "memory");
+  }
+  const bool staged = stageTable(p, b.tab);
+  __syncthreads();
+  return staged;
+}
+
+// One region of cycle t for this block: its items, then the region's side
+// work (digests and retiring-stream capture in region 0; memory reset of
+// retiring streams, next cycle's inputs and digest folding in region 1).
+template <int SPW, int G>
+__device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t r, bool event, uint32_t ev,
+                           uint32_t cEnd, uint32_t c0) {
+  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
+  const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
+  const uint32_t i0 = __ldg(ib + blockIdx.x), i1 = __ldg(ib + blockIdx.x + 1);
+  for (uint32_t i = i0; i < i1; ++i) {
+    const long long tk = clock64();
+    const uint32_t item = __ldg(p.items + i);
+    evalItem<SPW, G>(p, item, b.vp, b.tab, b.st, t, (event && r == 1) ? p.retireMask : nullptr);
+    // per-partition clock64 profile (SimEval.cu:894-983): running mean of the
+    // useful ticks over cycles [100, 200) of a launch, group block 0
+    if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {
+      const uint32_t pid = item & 0xFFFFFu, pc = t - c0 - 100;
+      p.profUseful[pid] = (p.profUseful[pid] * pc + (clock64() - tk)) / (pc + 1);
+    }
+  }
+  if (r == 0) {
+    if ((p.flags & kFlagDigest) || event) digestSlice<SPW>(p, t);
+    if (event) eventRegion0<SPW>(p, ev);
+  } else {
+    if (event) eventRegion1(p, ev, gtid, gthreads);
+    if ((p.flags & kFlagStimulus) && t + 1 < cEnd) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
+    if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
+  }
+}
+
+// Persistent form: every cycle of the launch, regions separated by the
+// bounded grid barrier.
 template <int SPW, int G>
 __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0, uint32_t nCycles) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) unsigned long long stageMbar[2];
-  uint8_t *tab = smem;
-  Stage st;
-  st.buf[0] = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
-  st.buf[1] = st.buf[0] + p.stageWords;
-  st.mb[0] = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
-  st.mb[1] = uint32_t(__cvta_generic_to_shared(&stageMbar[1]));
-  st.uses[0] = st.uses[1] = 0;
-  uint32_t *vp = st.buf[1] + p.stageWords;
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st.mb[0]) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st.mb[1]) : "memory");
-  }
-  const bool staged = stageTable(p, tab);
-  __syncthreads();
-  if (!staged) return;
+  BlockSmem b;
+  if (!setupBlock(p, smem, stageMbar, b)) return;
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
+  const uint32_t cEnd = c0 + nCycles;
   uint32_t gen = 0;
   if (p.flags & kFlagStimulus) {
     applyStimulus<SPW>(p, c0, gtid, gthreads);
@@ -801,37 +846,18 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
   }
   uint32_t ev = 0;
   const bool slots = (p.flags & kFlagSlots) != 0;
-  for (uint32_t t = c0; t < c0 + nCycles; ++t) {
+  for (uint32_t t = c0; t < cEnd; ++t) {
     const bool event = slots && ev < p.nEvents && __ldg(p.events + ev) == t;
 #pragma unroll 1
     for (uint32_t r = 0; r < 2; ++r) {
-      const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
-      const uint32_t b = __ldg(ib + blockIdx.x), e = __ldg(ib + blockIdx.x + 1);
       const long long tStart = clock64();
-      for (uint32_t i = b; i < e; ++i) {
-        const long long t0 = clock64();
-        const uint32_t item = __ldg(p.items + i);
-        evalItem<SPW, G>(p, item, vp, tab, st, t, (event && r == 1) ? p.retireMask : nullptr);
-        // per-partition clock64 profile (SimEval.cu:894-983): running mean of
-        // the useful ticks over cycles [100, 200) of group block 0
-        if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {
-          const uint32_t pid = item & 0xFFFFFu, pc = t - c0 - 100;
-          const long long useful = clock64() - t0;
-          p.profUseful[pid] = (p.profUseful[pid] * pc + useful) / (pc + 1);
-        }
-      }
-      if (r == 0 && ((p.flags & kFlagDigest) || event)) digestSlice<SPW>(p, t);
-      if (r == 0 && event) eventRegion0<SPW>(p, ev);
-      if (r == 1) {
-        if (event) eventRegion1(p, ev, gtid, gthreads);
-        if ((p.flags & kFlagStimulus) && t + 1 < c0 + nCycles) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
-        if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
-      }
+      regionWork<SPW, G>(p, b, t, r, event, ev, cEnd, c0);
       if (!gridSync(p, gen)) return;
       if ((p.flags & kFlagProfile) && threadIdx.x == 0 && t >= c0 + 100 && t < c0 + 200) {
         const long long total = clock64() - tStart;
         const uint32_t pc = t - c0 - 100;
-        for (uint32_t i = b; i < e; ++i) {
+        const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
+        for (uint32_t i = __ldg(ib + blockIdx.x); i < __ldg(ib + blockIdx.x + 1); ++i) {
           const uint32_t item = __ldg(p.items + i);
           if ((item >> 20) != 0) continue;
           const uint32_t pid = item & 0xFFFFFu;
@@ -846,6 +872,44 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
     }
     if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
   }
+}
+
+// Graph form: one launch per region, kernel boundaries instead of the grid
+// barrier; cycle = device counter + k so one captured chunk is replayed.
+template <int SPW, int G>
+__global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k, uint32_t r) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) unsigned long long stageMbar[2];
+  // graph state and the error word are written only by earlier launches
+  const uint32_t t = __ldcg(p.graphState) + k, cEnd = __ldcg(p.graphState + 2);
+  if (t >= cEnd || __ldcg(p.err)) return;
+  BlockSmem b;
+  if (!setupBlock(p, smem, stageMbar, b)) return;
+  const uint32_t ev = __ldcg(p.graphState + 1);
+  const bool event = (p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t;
+  regionWork<SPW, G>(p, b, t, r, event, ev, cEnd, __ldcg(p.graphState + 3));
+}
+
+// Graph form, after region 1: admission of the cycle's event (one block),
+// cycle bookkeeping.
+template <int SPW>
+__global__ void admitKernel(const KParams p, uint32_t k) {
+  const uint32_t t = __ldcg(p.graphState) + k;
+  if (t >= __ldcg(p.graphState + 2) || __ldcg(p.err)) return;
+  const uint32_t ev = __ldcg(p.graphState + 1);
+  if ((p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t) {
+    eventAdmit<SPW>(p, ev, t, threadIdx.x, blockDim.x);
+    __syncthreads();
+    if (threadIdx.x == 0) p.graphState[1] = ev + 1;
+  }
+  if ((p.flags & kFlagCountCycles) && threadIdx.x == 0) *p.realCycles += 1;
+}
+
+__global__ void advanceKernel(uint32_t *counter, uint32_t k) { *counter += k; }
+
+template <int SPW>
+__global__ void stimulusKernel(const KParams p, uint32_t cycle) {
+  applyStimulus<SPW>(p, cycle, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---- state utilities -----------------------------------------------------------
@@ -937,6 +1001,49 @@ cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint
   KParams pp = p;
   void *args[] = {&pp, &c0, &n};
   return cudaLaunchCooperativeKernel(fn, dim3(c.blocks), dim3(c.threads), args, c.smem, c.stream);
+}
+
+void *regionKernelFor(int spw, int G) {
+  if (spw == 1) return reinterpret_cast<void *>(&regionKernel<1, 1>);
+  if (G == 4) return reinterpret_cast<void *>(&regionKernel<8, 4>);
+  if (G == 2) return reinterpret_cast<void *>(&regionKernel<8, 2>);
+  return reinterpret_cast<void *>(&regionKernel<8, 1>);
+}
+
+// Enqueues one chunk of k cycles in graph form on the stream (captured by
+// the caller): per cycle region 0, region 1 and (admission / cycle count)
+// the admit kernel; then the cycle counter advance.
+cudaError_t enqueueGraphChunk(const LaunchCfg &c, const KParams &p, uint32_t k, bool admit) {
+  void *fn = regionKernelFor(c.spw, c.G);
+  KParams pp = p;
+  for (uint32_t i = 0; i < k; ++i) {
+    for (uint32_t r = 0; r < 2; ++r) {
+      uint32_t ki = i, ri = r;
+      void *args[] = {&pp, &ki, &ri};
+      cudaError_t e = cudaLaunchKernel(fn, dim3(c.blocks), dim3(c.threads), args, c.smem, c.stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (admit) {
+      if (c.spw == 8)
+        admitKernel<8><<<1, 256, 0, c.stream>>>(p, i);
+      else
+        admitKernel<1><<<1, 256, 0, c.stream>>>(p, i);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+  }
+  advanceKernel<<<1, 1, 0, c.stream>>>(p.graphState, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launchStimulus(int spw, const KParams &p, uint32_t cycle, cudaStream_t st) {
+  const uint32_t n = std::max<uint32_t>(1, p.nStim * p.gpad);
+  const uint32_t blocks = std::min<uint32_t>(1024, (n + 255) / 256);
+  if (spw == 8)
+    stimulusKernel<8><<<blocks, 256, 0, st>>>(p, cycle);
+  else
+    stimulusKernel<1><<<blocks, 256, 0, st>>>(p, cycle);
+  return cudaGetLastError();
 }
 
 cudaError_t launchInitState(int spw, const KParams &p, cudaStream_t st) {

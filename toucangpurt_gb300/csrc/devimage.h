@@ -131,6 +131,10 @@ struct KParams {
   // per-micro-partition clock64 profile (kFlagProfileMP), indexed by the id in header word 1
   unsigned long long *mpCycles;
   uint32_t *mpCount;
+  // graph form: cycle counter, event cursor, end cycle and first cycle of the run
+  // graph form: {cycle counter, event cursor, end cycle, first cycle} on the
+  // device, so one captured chunk serves every call
+  uint32_t *graphState;
 };
 
 constexpr uint32_t kNoStream = 0xFFFFFFFFu;

@@ -17,6 +17,9 @@ struct LaunchCfg {
 };
 
 void *cycleKernelFor(int spw, int G);
+void *regionKernelFor(int spw, int G);
+cudaError_t enqueueGraphChunk(const LaunchCfg &c, const KParams &p, uint32_t k, bool admit);
+cudaError_t launchStimulus(int spw, const KParams &p, uint32_t cycle, cudaStream_t st);
 cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint32_t n);
 cudaError_t launchInitState(int spw, const KParams &p, cudaStream_t st);
 cudaError_t launchRegDigest(int spw, const uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t nStreams,

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(32 * kWarps) mlpGradKernel(const float *__rest
     for (int wv = 0; wv < kWarps; ++wv) s += gacc[wv * kGradPad + src];
     atomicAdd(grad + i, s);
   }
-  for (int off = 16; off > 0; off >>= 1) lossAcc += __shfl_xor_sync(kFull, lossAcc, off);
+  // every lane of a warp holds the same output, so lane 0's sum is the warp's
   if (lane == 0 && loss) atomicAdd(loss, lossAcc);
 }
 

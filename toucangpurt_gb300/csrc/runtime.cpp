@@ -108,6 +108,15 @@ struct tgs_sim {
   tgs::DBuf<unsigned long long> jobSeed, memAcc, outReg, outMem, outRoll;
   tgs::DBuf<uint8_t> stimTable;
   tgs::DBuf<unsigned long long> mpCycles;
+  tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, event cursor, end, first cycle
+  // instantiated graph chunks, keyed by the launch parameters they captured
+  struct GraphEntry {
+    std::vector<uint8_t> key;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<GraphEntry> graphs;
+  uint64_t graphLaunches = 0;
+  uint32_t lastLaunches = 0;  // kernel launches of the last cycle run
   tgs::DBuf<uint32_t> mpCount;
   uint64_t batchCycle = 0;  // cycles run by TGS_BATCH_CONTINUE batches since the last reset
   tgs::DBuf<uint8_t> ioBytes;
@@ -117,6 +126,7 @@ struct tgs_sim {
 
   ~tgs_sim() {
     if (device >= 0) cudaSetDevice(device);
+    for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
     for (auto &m : msgs) m.free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -124,6 +134,8 @@ struct tgs_sim {
 
 namespace tgs {
 namespace {
+
+float runTimed(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags);
 
 void checkDeviceError(tgs_sim *h) {
   uint32_t info[4] = {0, 0, 0, 0};
@@ -233,6 +245,8 @@ void configure(tgs_sim *h) {
     h->lc.smem = kLutTablePadded + 2 * size_t(stage) * 4 + vpBytes;
     if (h->lc.smem > optin) return 0;
     TGS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
+    TGS_CUDA(cudaFuncSetAttribute(regionKernelFor(int(h->spw), G), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(h->lc.smem)));
     int perSM = 0;
     TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, int(h->lc.threads), h->lc.smem));
     if (o.blocks_per_sm) perSM = std::min<int>(perSM, int(o.blocks_per_sm));
@@ -328,6 +342,7 @@ void upload(tgs_sim *h) {
     TGS_CUDA(cudaMemcpyAsync(h->initMems.p, h->design.memPool.data(), h->design.memPool.size(), cudaMemcpyHostToDevice, s));
   h->err.alloc(1);
   h->errInfo.alloc(4);
+  h->graphState.alloc(4);
   h->barrier.alloc(2);
   h->realCycles.alloc(1);
   TGS_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(uint32_t), s));
@@ -375,11 +390,63 @@ void requireLoaded(tgs_sim *h) {
   TGS_CUDA(cudaSetDevice(h->device));
 }
 
+// Graph form: chunks of up to 32 cycles (two region launches and an admit
+// launch per cycle) captured once and replayed.  The kernels read the cycle,
+// the event cursor and the end cycle from device words, so a chunk captured
+// for one call serves every later call with the same launch parameters.
+cudaGraphExec_t graphChunk(tgs_sim *h, const KParams &p, uint32_t k, bool admit) {
+  std::vector<uint8_t> key(sizeof(KParams) + 7 * sizeof(uint32_t));
+  std::memcpy(key.data(), &p, sizeof(KParams));
+  const uint32_t tail[7] = {k, admit ? 1u : 0u, uint32_t(h->lc.spw), uint32_t(h->lc.G), h->lc.blocks, h->lc.threads,
+                            uint32_t(h->lc.smem)};
+  std::memcpy(key.data() + sizeof(KParams), tail, sizeof(tail));
+  for (auto &g : h->graphs)
+    if (g.key == key) return g.exec;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  TGS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t e = enqueueGraphChunk(h->lc, p, k, admit);
+  const cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    TGS_CUDA(e != cudaSuccess ? e : e2);
+  }
+  const cudaError_t e3 = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  TGS_CUDA(e3);
+  if (h->graphs.size() >= 4) {
+    cudaGraphExecDestroy(h->graphs.front().exec);
+    h->graphs.erase(h->graphs.begin());
+  }
+  h->graphs.push_back({std::move(key), exec});
+  return exec;
+}
+
+void runGraph(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
+  KParams p = h->kp;
+  p.graphState = h->graphState.p;
+  const uint32_t state[4] = {c0, 0, c0 + n, c0};
+  TGS_CUDA(cudaMemcpyAsync(h->graphState.p, state, sizeof(state), cudaMemcpyHostToDevice, h->stream));
+  if (flags & kFlagStimulus) TGS_CUDA(launchStimulus(int(h->spw), p, c0, h->stream));
+  const uint32_t k = std::min<uint32_t>(n, 32);
+  const bool admit = (flags & (kFlagSlots | kFlagCountCycles)) != 0;
+  cudaGraphExec_t exec = graphChunk(h, p, k, admit);
+  const uint32_t chunks = (n + k - 1) / k;
+  for (uint32_t i = 0; i < chunks; ++i) TGS_CUDA(cudaGraphLaunch(exec, h->stream));
+  h->graphLaunches += chunks;
+  h->lastLaunches = chunks * (k * (admit ? 3u : 2u) + 1u) + ((flags & kFlagStimulus) ? 1u : 0u);
+}
+
 void runCycles(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
   if (n == 0) return;
   h->kp.flags = flags;
+  if (h->opt.mode == TGS_MODE_GRAPH && !(flags & (kFlagProfile | kFlagProfileMP))) {
+    runGraph(h, c0, n, flags);
+    return;
+  }
   TGS_CUDA(cudaMemsetAsync(h->barrier.p, 0, 2 * sizeof(uint32_t), h->stream));
   TGS_CUDA(launchCycles(h->lc, h->kp, c0, n));
+  h->lastLaunches = 1;
 }
 
 int stopFlag(tgs_sim *h) {
@@ -510,6 +577,87 @@ int tgs_set_options(tgs_sim *h, const tgs_options *o) {
       configure(h);
       resetState(h);
     }
+  });
+}
+
+int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, uint32_t max_trials,
+                 uint32_t *n_trials, tgs_tune_trial *best) {
+  return guard([&] {
+    if (!h) throw Error(TGS_ERR_ARG, "null handle");
+    if (!h->loaded) throw Error(TGS_ERR_STATE, "tgs_autotune before tgs_init");
+    TGS_CUDA(cudaSetDevice(h->device));
+    tgs_tune_opts o{};
+    if (opts) o = *opts;
+    const uint32_t cycles = o.cycles ? o.cycles : 16, warm = o.warmup ? o.warmup : 2;
+    const uint32_t modes = o.modes ? o.modes : 3u;
+    const tgs_options base = h->opt;
+    std::vector<uint32_t> Gs = {1};
+    if (h->nStreams > 1) Gs = {1, 2, 4};
+    const uint32_t NWs[] = {4, 8, 16};
+    const uint32_t BPS[] = {1, 2, 0};
+    std::vector<tgs_tune_trial> all;
+    tgs_tune_trial win{};
+    win.ms_per_cycle = -1.f;
+    for (uint32_t G : Gs)
+      for (uint32_t NW : NWs)
+        for (uint32_t stagedOpt = 0; stagedOpt < (o.try_unstaged ? 2u : 1u); ++stagedOpt) {
+          uint32_t lastBlocks = 0;
+          for (uint32_t bps : BPS) {
+            tgs_options t = base;
+            t.groups_per_item = G;
+            t.warps_per_block = NW;
+            t.blocks_per_sm = bps;
+            t.resident_netlist = stagedOpt ? 2u : 0u;
+            h->opt = t;
+            tgs_tune_trial tr{G, NW, bps, 0, 0, 0, -1.f};
+            bool fits = true;
+            try {
+              configure(h);
+            } catch (const Error &e) {
+              if (e.code != TGS_ERR_RESOURCES && e.code != TGS_ERR_ARG) throw;
+              fits = false;
+            }
+            if (fits && h->lc.G != int(G)) fits = false;  // fewer groups than G: same as a smaller G
+            if (fits && h->lc.blocks == lastBlocks) continue;  // same grid as the previous trial
+            if (fits) lastBlocks = h->lc.blocks;
+            tr.blocks = fits ? h->lc.blocks : 0;
+            tr.staged = fits && h->stageWords ? 1u : 0u;
+            for (uint32_t mode = 0; mode < 2; ++mode) {
+              if (!(modes & (1u << mode))) continue;
+              tr.mode = mode;
+              tr.ms_per_cycle = -1.f;
+              if (fits) {
+                h->opt.mode = mode;
+                resetState(h);
+                fillParams(h);
+                runTimed(h, 0, warm, 0);
+                tr.ms_per_cycle = runTimed(h, warm, cycles, 0) / float(cycles);
+                if (win.ms_per_cycle < 0 || tr.ms_per_cycle < win.ms_per_cycle) win = tr;
+              }
+              all.push_back(tr);
+            }
+          }
+        }
+    if (win.ms_per_cycle < 0) {
+      h->opt = base;
+      configure(h);
+      resetState(h);
+      throw Error(TGS_ERR_RESOURCES, "no configuration fits");
+    }
+    h->opt = base;
+    h->opt.groups_per_item = win.groups_per_item;
+    h->opt.warps_per_block = win.warps_per_block;
+    h->opt.blocks_per_sm = win.blocks_per_sm;
+    h->opt.mode = win.mode;
+    h->opt.resident_netlist = win.staged ? 0u : (base.resident_netlist == 2 || o.try_unstaged ? 2u : 0u);
+    configure(h);
+    resetState(h);
+    h->cycleCnt = 0;
+    h->batchCycle = 0;
+    if (trials)
+      for (uint32_t i = 0; i < std::min<uint32_t>(max_trials, uint32_t(all.size())); ++i) trials[i] = all[i];
+    if (n_trials) *n_trials = uint32_t(all.size());
+    if (best) *best = win;
   });
 }
 
@@ -951,7 +1099,7 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
   for (uint32_t q = 0; q < n; ++q) total += job->cycles[q];
   res->device_ms = ms;
   res->stream_cycles = total;
-  res->launches = 1;
+  res->launches = h->lastLaunches;
   if (res->final_reg_digest) TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outReg.p, n * 8ull, cudaMemcpyDeviceToHost, st));
   if (res->final_mem_digest) TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outMem.p, n * 8ull, cudaMemcpyDeviceToHost, st));
   if (res->rolling_digest) TGS_CUDA(cudaMemcpyAsync(res->rolling_digest, h->outRoll.p, n * 8ull, cudaMemcpyDeviceToHost, st));
@@ -1036,7 +1184,7 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   if (!res) return;
   res->device_ms = ms;
   res->stream_cycles = uint64_t(cyc) * n;
-  res->launches = 1;
+  res->launches = h->lastLaunches;
   cudaStream_t s = h->stream;
   if (res->final_reg_digest || res->final_mem_digest) {
     TGS_CUDA(cudaMemsetAsync(h->outA.p, 0, n * 8ull, s));

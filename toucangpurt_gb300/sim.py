@@ -125,6 +125,17 @@ class Simulator:
         check(lib().tgs_copy_profile_data(self._h, _ptr(u, C.c_int64), _ptr(t, C.c_int64), n_parts))
         return u, t
 
+    def autotune(self, cycles: int = 16, warmup: int = 2, modes: int = 0, try_unstaged: bool = False):
+        """Times the launch configurations on the loaded design; keeps the
+        fastest (options updated, state reset).  Returns (best, trials) as dicts."""
+        o = capi.TuneOpts(cycles, warmup, modes, int(try_unstaged))
+        trials = (capi.TuneTrial * 256)()
+        n, best = C.c_uint32(), capi.TuneTrial()
+        check(lib().tgs_autotune(self._h, C.byref(o), trials, 256, C.byref(n), C.byref(best)))
+        conv = lambda t: {f: getattr(t, f) for f, _ in capi.TuneTrial._fields_}
+        check(lib().tgs_get_options(self._h, C.byref(self._opt)))
+        return conv(best), [conv(trials[i]) for i in range(min(n.value, 256))]
+
     def design_stats(self) -> dict:
         st = capi.DesignStats()
         check(lib().tgs_get_design_stats(self._h, C.byref(st)))
