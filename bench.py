@@ -48,6 +48,8 @@ def args_parse():
     p.add_argument("--warps", type=int, default=8)
     p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
     p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
+    p.add_argument("--value-pool", default="compact", choices=["compact", "design"],
+                   help="value-pool slots renumbered by live range (default) or as numbered in the design file")
     p.add_argument("--autotune", action="store_true", help="time the launch configurations first and keep the fastest")
     p.add_argument("--mode", default="persistent", choices=["persistent", "graph"],
                    help="cycle loop as one persistent launch or as replayed CUDA-graph chunks (one launch per region)")
@@ -281,7 +283,7 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     from toucangpurt_gb300 import sim, workloads
 
     s = sim.Simulator(n_streams=a.slots or 1024, groups_per_item=a.groups, warps_per_block=a.warps,
-                      mode=1 if a.mode == "graph" else 0)
+                      mode=1 if a.mode == "graph" else 0, value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
     cyc = workloads.stream_lengths(a.workload, streams, seed=7 + rank)
@@ -333,7 +335,8 @@ def run_gb300(a, rank, ws):
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
         return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
     s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=2 if a.no_stage else 0, mode=1 if a.mode == "graph" else 0)
+                      resident_netlist=2 if a.no_stage else 0, mode=1 if a.mode == "graph" else 0,
+                      value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
     st = s.design_stats()
@@ -375,7 +378,8 @@ def run_gb300(a, rank, ws):
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams, {cps} cycles per step",
                        "streams": streams, "cycles_per_step": cps, "lut_ops": st["lut_ops"],
                        "partitions": st["partitions"], "schedule": a.schedule, "groups_per_item": st["groups_per_item"],
-                       "mode": ["persistent", "graph"][s.options()["mode"]], **notes,
+                       "mode": ["persistent", "graph"][s.options()["mode"]], "value_pool": a.value_pool,
+                       "smem_per_block": st.get("smem_per_block"), **notes,
                        "threads_per_block": st["threads"], "blocks": st["blocks"],
                        "l2": "working set (memories) larger than L2"},
             "lut_evals_per_s": value * st["lut_ops"],

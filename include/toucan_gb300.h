@@ -67,7 +67,9 @@ typedef struct tgs_options {
   uint32_t barrier_timeout_ms; /* budget of every device-side wait (default 2000) */
   uint32_t validate;         /* 1 = run the static design checks at init (default 1) */
   uint32_t resident_netlist; /* 0: stage each exec level into shared memory when it fits (default); 2: read levels from global memory */
-  uint32_t reserved[7];
+  uint32_t value_pool;       /* 0: renumber value-pool slots by live range (default); 1: the design file's numbering.
+                                Takes effect at the next tgs_init / tgs_init_from_memory */
+  uint32_t reserved[6];
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u
@@ -246,7 +248,9 @@ typedef struct tgs_design_stats {
   uint32_t blocks, threads, groups_per_item, streams_per_word;
   uint64_t block_barriers, exec_levels;   /* block barriers kept / exec levels, all partitions */
   double makespan[2];        /* scheduled cost of the slowest block per region */
-  uint32_t reserved[8];
+  uint32_t smem_per_block;   /* dynamic shared memory of a block: table, stage buffers, value pool */
+  uint32_t stage_words;      /* words of one exec-level stage buffer (0: levels read from global memory) */
+  uint32_t reserved[6];
 } tgs_design_stats;
 int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *out);
 
@@ -342,6 +346,12 @@ int tgs_initial_state(const char *design_path, const char *symbol_path, int rand
  * independent of the schedule (def-before-use, no same-level slot conflicts,
  * word-aligned block copies, table bounds, nibble-valued tables). */
 int tgs_validate_file(const char *design_path, const char *symbol_path, uint64_t *lut_ops);
+
+/* Writes the design with every partition's value-pool slots renumbered by
+ * live range, the relabelling tgs_init applies to the device image when the
+ * value_pool option is 0 (no counterpart in the reference).  max_before /
+ * max_after (optional): the largest valuePoolSize before and after. */
+int tgs_compact_design(const char *in_path, const char *out_path, uint32_t *max_before, uint32_t *max_after);
 
 #ifdef __cplusplus
 }

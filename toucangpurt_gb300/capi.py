@@ -39,7 +39,7 @@ class Options(C.Structure):
         ("n_streams", C.c_uint32), ("warps_per_block", C.c_uint32), ("groups_per_item", C.c_uint32),
         ("blocks_per_sm", C.c_uint32), ("schedule", C.c_uint32), ("mode", C.c_uint32),
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
-        ("reserved", C.c_uint32 * 7),
+        ("value_pool", C.c_uint32), ("reserved", C.c_uint32 * 6),
     ]
 
 
@@ -96,7 +96,8 @@ class DesignStats(C.Structure):
         ("op_slots", C.c_uint64), ("partitions", C.c_uint32), ("mparts", C.c_uint32), ("max_value_pool", C.c_uint32),
         ("max_exec_levels", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("groups_per_item", C.c_uint32), ("streams_per_word", C.c_uint32), ("block_barriers", C.c_uint64),
-        ("exec_levels", C.c_uint64), ("makespan", C.c_double * 2), ("reserved", C.c_uint32 * 8),
+        ("exec_levels", C.c_uint64), ("makespan", C.c_double * 2), ("smem_per_block", C.c_uint32),
+        ("stage_words", C.c_uint32), ("reserved", C.c_uint32 * 6),
     ]
 
 
@@ -171,6 +172,7 @@ SIGNATURES = {
     "tgs_generate": [C.POINTER(GenConfig), C.c_char_p, C.c_char_p, C.POINTER(GenInfo)],
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
+    "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_resave_design": [C.c_char_p, C.c_char_p],
     "tgs_resave_symbols": [C.c_char_p, C.c_char_p],
     "tgs_initial_state": [C.c_char_p, C.c_char_p, C.c_int, u8p, C.c_size_t, u8p, C.c_size_t],

@@ -292,6 +292,7 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
   const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
   const bool multi = (hi >> 31) != 0;
   const uint32_t en = w2 & 0xFFFFu, av = w2 >> 16;
+  if (en == 0) return;  // immediate 0: neither reads nor writes (SimEval.cu:559-560)
 #pragma unroll 1
   for (int g = 0; g < G; ++g) {
     const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
@@ -491,7 +492,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     }
     for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
       const uint32_t opi = i / G, g = i % G;
-      const uint32_t en = __ldg(p.net + d.stopOff + opi);
+      const uint32_t sw = __ldg(p.net + d.stopOff + opi), en = sw & 0xFFFFu;
       const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
       for (int k = 0; k < SPW; ++k) {
         const uint32_t s = (gb * G + g) * SPW + k;
@@ -499,7 +500,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
         if (atomicExch(p.stop + s, 1u) == 0u) {
           p.stopCycle[s] = cycle;
           if (p.printDiag) {
-            printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, en, nib(EN, k));
+            printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, sw >> 16, nib(EN, k));
             for (uint32_t q = 0; q < d.printCount; ++q) {
               const uint32_t w = __ldg(p.net + d.printOff + q);
               if ((w & 0xFFFFu) == en && (w >> 16) < p.nPrintMsgs)

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "emit.h"
+#include "slotalloc.h"
 
 namespace tgs {
 
@@ -169,7 +170,7 @@ void accessOf(const CGMicroPartInfo &m, std::vector<uint32_t> &rd, std::vector<u
 
 }  // namespace
 
-void buildImage(const SimDesignInfo &d, DeviceImage &img) {
+void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots) {
   img = DeviceImage();
   img.parts.resize(d.parts.size());
   img.mp.resize(d.parts.size());
@@ -178,7 +179,19 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img) {
     for (uint32_t id : d.regionPartitionIds[r]) img.partRegion[id] = uint32_t(r);
   auto &net = img.net;
   for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
-    const SimPartitionInfo &p = d.parts[pid];
+    const SimPartitionInfo &orig = d.parts[pid];
+    SimPartitionInfo renamed;
+    const SimPartitionInfo *pp = &orig;
+    if (compactSlots) {
+      std::vector<uint32_t> newOf;
+      const uint32_t n = planSlots(orig, newOf);
+      if (n <= 65534) {
+        renamed = orig;
+        renameSlots(renamed, newOf, n);
+        pp = &renamed;
+      }
+    }
+    const SimPartitionInfo &p = *pp;
     PartDesc &pd = img.parts[pid];
     std::memset(&pd, 0, sizeof(pd));
     pd.vpSlots = (std::max<uint32_t>(p.valuePoolSize, 16) + 3) & ~3u;
@@ -265,7 +278,9 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img) {
       for (auto &pr : p.ops_last_print) net.push_back(uint32_t(pr.en) | (uint32_t(pr.msg) << 16));
       pd.stopCount = uint32_t(p.ops_last_stop.size());
       pd.stopOff = uint32_t(net.size());
-      for (auto &st : p.ops_last_stop) net.push_back(uint32_t(st.en));
+      // enable slot | the design file's number of it (for the stop diagnostic)
+      for (size_t i = 0; i < p.ops_last_stop.size(); ++i)
+        net.push_back(uint32_t(p.ops_last_stop[i].en) | (uint32_t(orig.ops_last_stop[i].en) << 16));
     }
     pd.constOff = uint32_t(img.constVec.size());
     pd.constLen = uint32_t(p.constVecPool.size());

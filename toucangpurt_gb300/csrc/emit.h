@@ -60,7 +60,8 @@ struct Schedule {
   uint64_t barriers = 0, levels = 0;
 };
 
-void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img);
+// compactSlots: renumber value-pool slots by live range (slotalloc.h)
+void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
 void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW,
                    const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "emit.h"
+#include "slotalloc.h"
 #include "kernels.h"
 #include "learned.h"
 #include "tgs_internal.h"
@@ -326,7 +327,7 @@ void setupDevice(tgs_sim *h, int gpu) {
 
 void upload(tgs_sim *h) {
   cudaStream_t s = h->stream;
-  buildImage(h->design, h->img);
+  buildImage(h->design, h->img, h->opt.value_pool == 0);
   h->net.upload(h->img.net, s);
   h->constVec.upload(h->img.constVec, s);
   std::vector<uint8_t> lut(kLutTablePadded, 0);
@@ -1273,6 +1274,8 @@ extern "C" int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *o) {
     o->exec_levels = h->sched.levels;
     o->makespan[0] = h->sched.makespan[0];
     o->makespan[1] = h->sched.makespan[1];
+    o->smem_per_block = uint32_t(h->lc.smem);
+    o->stage_words = h->stageWords;
   });
 }
 
@@ -1282,6 +1285,28 @@ extern "C" int tgs_resave_design(const char *in, const char *out) {
     auto bytes = readFileBytes(in);
     SimDesignInfo d;
     parseDesign(bytes.data(), bytes.size(), d);
+    std::ofstream o(out, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
+    serializeSimDesignInfo(o, d);
+  });
+}
+
+extern "C" int tgs_compact_design(const char *in, const char *out, uint32_t *maxBefore, uint32_t *maxAfter) {
+  return guard([&] {
+    if (!in || !out) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(in);
+    SimDesignInfo d;
+    parseDesign(bytes.data(), bytes.size(), d);
+    uint32_t before = 0, after = 0;
+    for (auto &p : d.parts) {
+      before = std::max(before, p.valuePoolSize);
+      std::vector<uint32_t> newOf;
+      const uint32_t n = planSlots(p, newOf);
+      if (n <= 65534) renameSlots(p, newOf, n);
+      after = std::max(after, p.valuePoolSize);
+    }
+    if (maxBefore) *maxBefore = before;
+    if (maxAfter) *maxAfter = after;
     std::ofstream o(out, std::ios::binary);
     if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
     serializeSimDesignInfo(o, d);

@@ -1,0 +1,18 @@
+// Value-pool slot allocation (see slotalloc.cpp).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "ToucanGPUGenDataTypes.h"
+
+namespace tgs {
+
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+
+// New number of every slot of the partition (kNoSlot: never accessed);
+// returns the new pool size.
+uint32_t planSlots(const toucanGPUSim::SimPartitionInfo &p, std::vector<uint32_t> &newOf);
+// Rewrites every slot reference of the partition through newOf.
+void renameSlots(toucanGPUSim::SimPartitionInfo &p, const std::vector<uint32_t> &newOf, uint32_t newSize);
+
+}  // namespace tgs
