@@ -122,6 +122,12 @@ int tgs_eval(tgs_sim *h, int *stop);
 /* ToucanSimulator::eval_free_running (src/ToucanSim.cu:232-267): `cycles`
  * cycles in one persistent launch; like the reference it does not stop early. */
 int tgs_eval_free_running(tgs_sim *h, uint32_t cycles, int *stop);
+/* Free running with the early exit the reference leaves commented out
+ * (src/SimEval.cu:990-992): a stream that executes a stop op freezes after
+ * that cycle and the launch ends once every stream stopped, or after
+ * max_cycles.  *cycles_run = cycles executed (added to cycle_cnt and
+ * realCycles).  No counterpart in the reference. */
+int tgs_eval_until_stop(tgs_sim *h, uint32_t max_cycles, int *stop, uint32_t *cycles_run);
 
 /* ToucanSimulator::setRegister / readRegister (src/ToucanSim.cu:271-289,
  * src/SimEval.cu:1058-1081): value split into nibbles, most significant
@@ -162,6 +168,17 @@ int tgs_state_digest(tgs_sim *h, uint32_t stream, uint64_t *reg_digest, uint64_t
 /* Reset every stream to the initial state (Init/Randomize result). */
 int tgs_reset_state(tgs_sim *h);
 
+/* Checkpoint (no counterpart in the reference): every stream's register and
+ * memory pools, stop flags, stop cycles and rolling digests, plus the cycle
+ * counters, written to a file in a layout independent of the launch options.
+ * tgs_load_state restores it into a handle holding the same design (checked
+ * by a fingerprint of the design's structure); the handle takes the file's
+ * stream count.  A run continued after a load (eval, eval_free_running,
+ * tgs_batch_run with TGS_BATCH_CONTINUE) gives the results of the run that
+ * was never interrupted. */
+int tgs_dump_state(tgs_sim *h, const char *path);
+int tgs_load_state(tgs_sim *h, const char *path);
+
 /* Same digest as tgs_state_digest, of caller-owned device memory, for
  * callers that cannot allocate device memory (an allocator that owns every
  * device byte, a frozen memory pool).  No counterpart in the reference.
@@ -189,9 +206,10 @@ typedef struct tgs_stimulus {
   const uint8_t *bits;     /* bit width of each input nibble (1..4) */
   const uint16_t *toggle;  /* NULL = all inputs uniform */
   /* Optional host table of input values, [cycle][input][stream] one nibble
-   * per byte, covering the cycles of this call (runs where every stream is
-   * resident and equally long); replaces the seeded values.  Pinned memory
-   * (tgs_host_alloc) makes the upload faster. */
+   * per byte (written to the register nibble as is), covering the cycles of
+   * this call (runs where every stream is resident and equally long);
+   * replaces the seeded values.  Pinned memory (tgs_host_alloc) makes the
+   * upload faster. */
   const uint8_t *table;
 } tgs_stimulus;
 
@@ -199,6 +217,9 @@ typedef struct tgs_stimulus {
 #define TGS_BATCH_ROLLING 2u       /* fill rolling_digest[] */
 #define TGS_BATCH_FINAL_STATE 4u   /* fill final_regs[] / final_mems[] */
 #define TGS_BATCH_CONTINUE 8u      /* continue every stream from the previous call's state and cycle */
+#define TGS_BATCH_STOP_EXIT 16u    /* a stream that executes a stop op freezes after that cycle (registers,
+                                      memories, digests); the launch ends once every stream stopped.
+                                      Streams must all be resident (no queueing). */
 
 typedef struct tgs_batch {
   uint32_t n_streams;       /* streams in the job (may exceed resident slots) */

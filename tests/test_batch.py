@@ -33,6 +33,53 @@ def test_host_table_matches_device_hash(batch_design):
                 assert tab[c, i, s] == h & ((1 << int(info["pi_bits"][i])) - 1)
 
 
+def test_host_table_toggles_follow_device_rule(batch_design):
+    """Toggle inputs in the host table flip the previous value exactly when
+    the device would (h >> 48 < toggle)."""
+    from oracle import pyoracle as po
+
+    dp, sp, info = batch_design
+    ids, bits = info["pi_ids"], info["pi_bits"]
+    tog = np.where(np.arange(len(ids)) % 2 == 0, 20000, 0).astype(np.uint16)
+    spec = sim.StimulusSpec(9, ids, bits, tog)
+    n, c0, cyc = 3, 4, 5
+    prev = (np.arange(len(ids) * n, dtype=np.uint8).reshape(len(ids), n) & 15)
+    tab = sim.stimulus_table(spec, n, c0, cyc, prev=prev)
+    seeds = [po.lib().orc_mix64(9 ^ s) for s in range(n)]
+    cur = prev.astype(int).copy()
+    for c in range(cyc):
+        for i in range(len(ids)):
+            mask = (1 << int(bits[i])) - 1
+            for s in range(n):
+                h = po.lib().orc_mix64(seeds[s] ^ po.lib().orc_mix64(((c0 + c) << 32) | i))
+                if tog[i]:
+                    cur[i, s] = cur[i, s] ^ mask if (h >> 48) < tog[i] else cur[i, s]
+                else:
+                    cur[i, s] = h & mask
+                assert tab[c, i, s] == cur[i, s]
+
+
+@pytest.mark.gpu
+def test_toggle_tables_match_seeded_run(batch_design):
+    """Continued calls fed by toggle-aware host tables equal one seeded run."""
+    dp, sp, info = batch_design
+    n, steps, per = 16, 3, 11
+    tog = workloads.toggles("batch", info["pi_bits"])
+    spec = sim.StimulusSpec(21, info["pi_ids"], info["pi_bits"], tog)
+    with sim.Simulator(n_streams=n) as s:
+        s.init(0, dp, sp, False, False)
+        prev = np.repeat(s.reg_pool(0)[info["pi_ids"]][:, None], n, axis=1)
+        for k in range(steps):
+            tab = sim.stimulus_table(spec, n, k * per, per, prev=prev)
+            prev = tab[-1]
+            tspec = sim.StimulusSpec(21, info["pi_ids"], info["pi_bits"], table=tab)
+            got = s.batch_run(np.full(n, per, np.uint32), tspec, continue_=k > 0, final_digests=k == steps - 1)
+    ref = pyoracle.OracleDesign(dp, sp).run(np.full(n, steps * per, np.uint32), spec)
+    np.testing.assert_array_equal(got.final_reg_digest, ref["final_reg_digest"])
+    np.testing.assert_array_equal(got.final_mem_digest, ref["final_mem_digest"])
+    np.testing.assert_array_equal(got.rolling_digest, ref["rolling_digest"])
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,slots", [(20, 8), (37, 16), (64, 64), (100, 24)])
 def test_admission_matches_oracle(batch_design, n, slots):

@@ -25,7 +25,7 @@ ERR_RESOURCES, ERR_TIMEOUT, ERR_STATE, ERR_NOT_FOUND, ERR_RANGE, ERR_DEVICE_FAUL
 
 SCHED_GREEDY, SCHED_LEARNED = 0, 1
 MODE_PERSISTENT, MODE_GRAPH = 0, 1
-BATCH_CYCLE_DIGESTS, BATCH_ROLLING, BATCH_FINAL_STATE, BATCH_CONTINUE = 1, 2, 4, 8
+BATCH_CYCLE_DIGESTS, BATCH_ROLLING, BATCH_FINAL_STATE, BATCH_CONTINUE, BATCH_STOP_EXIT = 1, 2, 4, 8, 16
 
 
 class TgsError(RuntimeError):
@@ -173,6 +173,9 @@ SIGNATURES = {
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
     "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
+    "tgs_dump_state": [C.c_void_p, C.c_char_p],
+    "tgs_eval_until_stop": [C.c_void_p, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_uint32)],
+    "tgs_load_state": [C.c_void_p, C.c_char_p],
     "tgs_resave_design": [C.c_char_p, C.c_char_p],
     "tgs_resave_symbols": [C.c_char_p, C.c_char_p],
     "tgs_initial_state": [C.c_char_p, C.c_char_p, C.c_int, u8p, C.c_size_t, u8p, C.c_size_t],

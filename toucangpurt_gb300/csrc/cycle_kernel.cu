@@ -437,7 +437,29 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
   uint32_t rm[G];
 #pragma unroll
   for (int g = 0; g < G; ++g) rm[g] = retire ? __ldcg(retire + gb * G + g) : 0u;
-  if (d.copyKind == 1 && retire) {
+  // stop exit: streams stopped in an earlier cycle keep their state; their
+  // register words are rewritten with the values they hold
+  const bool stopExit = (p.flags & kFlagStopExit) != 0;
+  uint32_t fm[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    fm[g] = 0;
+    if (stopExit) {
+#pragma unroll
+      for (int k = 0; k < SPW; ++k) {
+        const uint32_t s = (gb * G + g) * SPW + k;
+        if (s < p.nStreams && __ldcg(p.stopCycle + s) < cycle) fm[g] |= 15u << (4 * k);
+      }
+      rm[g] |= fm[g];
+    }
+  }
+  if (d.copyKind == 1 && stopExit) {
+    for (uint32_t i = tid; i < d.copySlots; i += nthr) {
+      uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
+#pragma unroll
+      for (int g = 0; g < G; ++g) dst[g] = (vp[(d.copySrc + i) * G + g] & ~fm[g]) | (__ldcg(dst + g) & fm[g]);
+    }
+  } else if (d.copyKind == 1 && retire) {
     for (uint32_t i = tid; i < d.copySlots; i += nthr) {
       const uint32_t iv = p.initRegs[d.copyDst + i];
       const uint32_t init = SPW == 8 ? rep8(iv) : iv;
@@ -499,6 +521,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
         if (s >= p.nStreams || nib(EN, k) == 0) continue;
         if (atomicExch(p.stop + s, 1u) == 0u) {
           p.stopCycle[s] = cycle;
+          if (stopExit) atomicAdd(p.nStopped, 1u);
           if (p.printDiag) {
             printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, sw >> 16, nib(EN, k));
             for (uint32_t q = 0; q < d.printCount; ++q) {
@@ -523,6 +546,7 @@ __device__ __forceinline__ bool stimValue(const KParams &p, uint32_t s, uint32_t
   uint32_t lc;
   unsigned long long seed;
   if (s >= p.nStreams) return false;  // padding slot of the last group
+  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;  // frozen after its stop
   if (p.flags & kFlagSlots) {
     const uint32_t q = __ldcg(p.slotStream + s);
     if (q == kNoStream || cycle >= __ldcg(p.slotRetire + s)) return false;
@@ -532,7 +556,7 @@ __device__ __forceinline__ bool stimValue(const KParams &p, uint32_t s, uint32_t
     lc = cycle;
     seed = __ldg(p.streamSeed + s);
     if (p.stimTable) {
-      v = __ldg(p.stimTable + (size_t(cycle - p.stimTableC0) * p.nStim + inp) * p.nStreams + s) & mask;
+      v = __ldg(p.stimTable + (size_t(cycle - p.stimTableC0) * p.nStim + inp) * p.nStreams + s) & 15u;
       return true;
     }
   }
@@ -570,6 +594,7 @@ __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, u
 // with per-cycle digests, else (admission) only the streams retiring now.
 __device__ __forceinline__ bool digestStream(const KParams &p, uint32_t s, uint32_t cycle) {
   if (s >= p.nStreams) return false;
+  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;
   if (!(p.flags & kFlagSlots)) return true;
   if (__ldcg(p.slotStream + s) == kNoStream) return false;
   return (p.flags & kFlagDigest) || __ldcg(p.slotRetire + s) == cycle;
@@ -612,6 +637,7 @@ __device__ void digestSlice(const KParams &p, uint32_t cycle) {
 __device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
   for (uint32_t s = gtid; s < p.nStreams; s += gthreads) {
     uint32_t q = s, lc = cycle - p.cycBase;
+    if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) continue;
     if (p.flags & kFlagSlots) {
       q = __ldcg(p.slotStream + s);
       if (q == kNoStream || __ldcg(p.slotRetire + s) == cycle) continue;  // retiring: kept for the admin phase
@@ -825,7 +851,8 @@ __device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t 
     if (event) eventRegion0<SPW>(p, ev);
   } else {
     if (event) eventRegion1(p, ev, gtid, gthreads);
-    if ((p.flags & kFlagStimulus) && t + 1 < cEnd) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
+    // (stop exit: applied after the region barrier, when every stop of the cycle is known)
+    if ((p.flags & kFlagStimulus) && !(p.flags & kFlagStopExit) && t + 1 < cEnd) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
     if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
   }
 }
@@ -871,7 +898,13 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
       ++ev;
       if (!gridSync(p, gen)) return;
     }
+    if ((p.flags & kFlagStopExit) && (p.flags & kFlagStimulus) && t + 1 < cEnd) {
+      applyStimulus<SPW>(p, t + 1, gtid, gthreads);
+      if (!gridSync(p, gen)) return;
+    }
     if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
+    // every block reads the count after the cycle's last barrier: same decision
+    if ((p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) break;
   }
 }
 
@@ -883,7 +916,7 @@ __global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k
   __shared__ __align__(8) unsigned long long stageMbar[2];
   // graph state and the error word are written only by earlier launches
   const uint32_t t = __ldcg(p.graphState) + k, cEnd = __ldcg(p.graphState + 2);
-  if (t >= cEnd || __ldcg(p.err)) return;
+  if (t >= cEnd || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
   BlockSmem b;
   if (!setupBlock(p, smem, stageMbar, b)) return;
   const uint32_t ev = __ldcg(p.graphState + 1);
@@ -896,14 +929,26 @@ __global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k
 template <int SPW>
 __global__ void admitKernel(const KParams p, uint32_t k) {
   const uint32_t t = __ldcg(p.graphState) + k;
-  if (t >= __ldcg(p.graphState + 2) || __ldcg(p.err)) return;
+  // graphState[4] (stop exit) is written only here, after the cycle's regions
+  if (t >= __ldcg(p.graphState + 2) || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
   const uint32_t ev = __ldcg(p.graphState + 1);
   if ((p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t) {
     eventAdmit<SPW>(p, ev, t, threadIdx.x, blockDim.x);
     __syncthreads();
     if (threadIdx.x == 0) p.graphState[1] = ev + 1;
   }
-  if ((p.flags & kFlagCountCycles) && threadIdx.x == 0) *p.realCycles += 1;
+  if (threadIdx.x == 0) {
+    if (p.flags & kFlagCountCycles) *p.realCycles += 1;
+    if ((p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) p.graphState[4] = 1;
+  }
+}
+
+// Graph form, stop exit: the next cycle's inputs, after the region-1 launch.
+template <int SPW>
+__global__ void graphStimulusKernel(const KParams p, uint32_t k) {
+  const uint32_t t = __ldcg(p.graphState) + k;
+  if (t + 1 >= __ldcg(p.graphState + 2) || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
+  applyStimulus<SPW>(p, t + 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 __global__ void advanceKernel(uint32_t *counter, uint32_t k) { *counter += k; }
@@ -1022,6 +1067,16 @@ cudaError_t enqueueGraphChunk(const LaunchCfg &c, const KParams &p, uint32_t k, 
       uint32_t ki = i, ri = r;
       void *args[] = {&pp, &ki, &ri};
       cudaError_t e = cudaLaunchKernel(fn, dim3(c.blocks), dim3(c.threads), args, c.smem, c.stream);
+      if (e != cudaSuccess) return e;
+    }
+    if ((p.flags & kFlagStopExit) && (p.flags & kFlagStimulus)) {
+      const uint32_t n = std::max<uint32_t>(1, p.nStim * p.gpad);
+      const uint32_t blocks = std::min<uint32_t>(1024, (n + 255) / 256);
+      if (c.spw == 8)
+        graphStimulusKernel<8><<<blocks, 256, 0, c.stream>>>(p, i);
+      else
+        graphStimulusKernel<1><<<blocks, 256, 0, c.stream>>>(p, i);
+      cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
     if (admit) {

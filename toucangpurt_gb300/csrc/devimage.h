@@ -132,9 +132,10 @@ struct KParams {
   unsigned long long *mpCycles;
   uint32_t *mpCount;
   // graph form: cycle counter, event cursor, end cycle and first cycle of the run
-  // graph form: {cycle counter, event cursor, end cycle, first cycle} on the
+  // graph form: {cycle counter, event cursor, end cycle, first cycle, exit} on the
   // device, so one captured chunk serves every call
   uint32_t *graphState;
+  uint32_t *nStopped;         // kFlagStopExit: streams stopped so far
 };
 
 constexpr uint32_t kNoStream = 0xFFFFFFFFu;
@@ -145,7 +146,8 @@ enum : uint32_t {
   kFlagProfile = 4u,    // per-partition clock64 profile (free-running)
   kFlagCountCycles = 8u, // advance realCycles (free-running launches only, SimEval.cu:985-989)
   kFlagSlots = 16u,      // job streams queued onto resident slots, retired and admitted in place
-  kFlagProfileMP = 32u   // clock64 cycles of every micro-partition evaluation (cost-model samples)
+  kFlagProfileMP = 32u,  // clock64 cycles of every micro-partition evaluation (cost-model samples)
+  kFlagStopExit = 64u    // a stream freezes after its stop cycle; the launch ends once every stream stopped
 };
 
 enum : uint32_t {

@@ -109,7 +109,8 @@ struct tgs_sim {
   tgs::DBuf<unsigned long long> jobSeed, memAcc, outReg, outMem, outRoll;
   tgs::DBuf<uint8_t> stimTable;
   tgs::DBuf<unsigned long long> mpCycles;
-  tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, event cursor, end, first cycle
+  tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, event cursor, end, first cycle, exit
+  tgs::DBuf<uint32_t> nStopped;    // stop exit: streams stopped
   // instantiated graph chunks, keyed by the launch parameters they captured
   struct GraphEntry {
     std::vector<uint8_t> key;
@@ -184,6 +185,7 @@ void fillParams(tgs_sim *h) {
   p.errInfo = h->errInfo.p;
   p.barrier = h->barrier.p;
   p.realCycles = h->realCycles.p;
+  p.nStopped = h->nStopped.p;
   p.digAcc = h->digAcc.p;
   p.roll = h->roll.p;
   p.cycDig = nullptr;
@@ -343,7 +345,8 @@ void upload(tgs_sim *h) {
     TGS_CUDA(cudaMemcpyAsync(h->initMems.p, h->design.memPool.data(), h->design.memPool.size(), cudaMemcpyHostToDevice, s));
   h->err.alloc(1);
   h->errInfo.alloc(4);
-  h->graphState.alloc(4);
+  h->graphState.alloc(5);
+  h->nStopped.alloc(1);
   h->barrier.alloc(2);
   h->realCycles.alloc(1);
   TGS_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(uint32_t), s));
@@ -423,26 +426,42 @@ cudaGraphExec_t graphChunk(tgs_sim *h, const KParams &p, uint32_t k, bool admit)
   return exec;
 }
 
-void runGraph(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
+void runGraph(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags, uint32_t stopped0) {
   KParams p = h->kp;
   p.graphState = h->graphState.p;
-  const uint32_t state[4] = {c0, 0, c0 + n, c0};
+  const uint32_t exit0 = (flags & kFlagStopExit) && stopped0 >= h->nStreams ? 1u : 0u;
+  const uint32_t state[5] = {c0, 0, c0 + n, c0, exit0};
   TGS_CUDA(cudaMemcpyAsync(h->graphState.p, state, sizeof(state), cudaMemcpyHostToDevice, h->stream));
-  if (flags & kFlagStimulus) TGS_CUDA(launchStimulus(int(h->spw), p, c0, h->stream));
+  if ((flags & kFlagStimulus) && !exit0) TGS_CUDA(launchStimulus(int(h->spw), p, c0, h->stream));
   const uint32_t k = std::min<uint32_t>(n, 32);
-  const bool admit = (flags & (kFlagSlots | kFlagCountCycles)) != 0;
+  const bool admit = (flags & (kFlagSlots | kFlagCountCycles | kFlagStopExit)) != 0;
   cudaGraphExec_t exec = graphChunk(h, p, k, admit);
   const uint32_t chunks = (n + k - 1) / k;
   for (uint32_t i = 0; i < chunks; ++i) TGS_CUDA(cudaGraphLaunch(exec, h->stream));
   h->graphLaunches += chunks;
-  h->lastLaunches = chunks * (k * (admit ? 3u : 2u) + 1u) + ((flags & kFlagStimulus) ? 1u : 0u);
+  const uint32_t perCycle = 2u + (admit ? 1u : 0u) + ((flags & kFlagStopExit) && (flags & kFlagStimulus) ? 1u : 0u);
+  h->lastLaunches = chunks * (k * perCycle + 1u) + ((flags & kFlagStimulus) ? 1u : 0u);
 }
 
 void runCycles(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
   if (n == 0) return;
+  uint32_t stopped0 = 0;
+  if (flags & kFlagStopExit) {
+    // streams that stopped before this launch count towards the exit
+    std::vector<uint32_t> st(h->nStreams);
+    TGS_CUDA(cudaMemcpyAsync(st.data(), h->stop.p, h->nStreams * 4ull, cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    for (uint32_t v : st) stopped0 += v != 0;
+    h->lastLaunches = 0;
+    if (stopped0 >= h->nStreams) return;  // every stream already stopped
+    TGS_CUDA(cudaMemcpyAsync(h->nStopped.p, &stopped0, 4, cudaMemcpyHostToDevice, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  // the graph form records no per-partition profile (persistent form only)
+  if (h->opt.mode == TGS_MODE_GRAPH && !(flags & kFlagProfileMP)) flags &= ~kFlagProfile;
   h->kp.flags = flags;
-  if (h->opt.mode == TGS_MODE_GRAPH && !(flags & (kFlagProfile | kFlagProfileMP))) {
-    runGraph(h, c0, n, flags);
+  if (h->opt.mode == TGS_MODE_GRAPH && !(flags & kFlagProfileMP)) {
+    runGraph(h, c0, n, flags, stopped0);
     return;
   }
   TGS_CUDA(cudaMemsetAsync(h->barrier.p, 0, 2 * sizeof(uint32_t), h->stream));
@@ -712,6 +731,21 @@ int tgs_eval_free_running(tgs_sim *h, uint32_t cycles, int *stop) {
   });
 }
 
+int tgs_eval_until_stop(tgs_sim *h, uint32_t max_cycles, int *stop, uint32_t *cycles_run) {
+  return guard([&] {
+    requireLoaded(h);
+    uint32_t r0 = 0, r1 = 0;
+    TGS_CUDA(cudaMemcpy(&r0, h->realCycles.p, 4, cudaMemcpyDeviceToHost));
+    runCycles(h, uint32_t(h->cycleCnt), max_cycles, kFlagCountCycles | kFlagStopExit);
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
+    checkDeviceError(h);
+    TGS_CUDA(cudaMemcpy(&r1, h->realCycles.p, 4, cudaMemcpyDeviceToHost));
+    h->cycleCnt += r1 - r0;
+    if (cycles_run) *cycles_run = r1 - r0;
+    if (stop) *stop = stopFlag(h);
+  });
+}
+
 int tgs_set_register(tgs_sim *h, const char *name, uint64_t value) {
   return guard([&] { requireLoaded(h); setRegister(h, 0, name, value); });
 }
@@ -838,6 +872,146 @@ int tgs_write_mem_pool(tgs_sim *h, uint32_t s, const uint8_t *in, size_t bytes) 
     if (!in || bytes != h->design.memPoolSize) throw Error(TGS_ERR_ARG, "buffer must hold memPoolSize bytes");
     if (s >= h->nStreams) throw Error(TGS_ERR_ARG, "stream index out of range");
     TGS_CUDA(cudaMemcpy(h->mems.p + size_t(s) * h->memStride, in, bytes, cudaMemcpyHostToDevice));
+  });
+}
+
+namespace {
+
+constexpr char kStateMagic[8] = {'T', 'G', 'S', 'S', 'T', 'A', 'T', 'E'};
+constexpr uint32_t kStateVersion = 1;
+
+struct StateHeader {
+  char magic[8];
+  uint32_t version, nStreams;
+  uint64_t fingerprint;
+  uint32_t regPoolSize, pad0;
+  uint64_t memPoolSize;
+  uint64_t cycleCnt, batchCycle;
+  uint32_t realCycles, pad1;
+};
+static_assert(sizeof(StateHeader) == 64, "state header");
+
+// Structure of the design (pool sizes, partitions, ops per level): enough to
+// refuse a checkpoint of another design.
+uint64_t designFingerprint(const SimDesignInfo &d) {
+  uint64_t h = 0x243F6A8885A308D3ull;
+  auto add = [&](uint64_t v) { h = mix64(h ^ v); };
+  add(d.regPoolSize);
+  add(d.memPoolSize);
+  add(d.exchangePoolSize);
+  add(d.parts.size());
+  for (const auto &p : d.parts) {
+    add(p.valuePoolSize);
+    add(p.ops_l0_regRead.size() | (uint64_t(p.ops_l0_exchangeRead.size()) << 32));
+    add(p.exec_mParts.size());
+    for (const auto &lv : p.exec_mParts) add(lv.size());
+  }
+  return h;
+}
+
+}  // namespace
+
+int tgs_dump_state(tgs_sim *h, const char *path) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!path) throw Error(TGS_ERR_ARG, "null path");
+    std::ofstream o(path, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + path);
+    const uint32_t n = h->nStreams;
+    StateHeader hd{};
+    std::memcpy(hd.magic, kStateMagic, 8);
+    hd.version = kStateVersion;
+    hd.nStreams = n;
+    hd.fingerprint = designFingerprint(h->design);
+    hd.regPoolSize = h->design.regPoolSize;
+    hd.memPoolSize = h->design.memPoolSize;
+    hd.cycleCnt = h->cycleCnt;
+    hd.batchCycle = h->batchCycle;
+    TGS_CUDA(cudaMemcpy(&hd.realCycles, h->realCycles.p, 4, cudaMemcpyDeviceToHost));
+    o.write(reinterpret_cast<const char *>(&hd), sizeof(hd));
+    std::vector<uint32_t> stop(n), stopCycle(n);
+    std::vector<unsigned long long> roll(n);
+    TGS_CUDA(cudaMemcpy(stop.data(), h->stop.p, n * 4ull, cudaMemcpyDeviceToHost));
+    TGS_CUDA(cudaMemcpy(stopCycle.data(), h->stopCycle.p, n * 4ull, cudaMemcpyDeviceToHost));
+    TGS_CUDA(cudaMemcpy(roll.data(), h->roll.p, n * 8ull, cudaMemcpyDeviceToHost));
+    o.write(reinterpret_cast<const char *>(stop.data()), n * 4ull);
+    o.write(reinterpret_cast<const char *>(stopCycle.data()), n * 4ull);
+    o.write(reinterpret_cast<const char *>(roll.data()), n * 8ull);
+    h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
+    std::vector<uint8_t> buf(std::max<size_t>(h->regSlots, size_t(1) << 24));
+    for (uint32_t st = 0; st < n; ++st) {
+      uint32_t g, k;
+      streamPos(h, st, g, k);
+      TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+      TGS_CUDA(cudaMemcpyAsync(buf.data(), h->ioBytes.p, hd.regPoolSize, cudaMemcpyDeviceToHost, h->stream));
+      TGS_CUDA(cudaStreamSynchronize(h->stream));
+      o.write(reinterpret_cast<const char *>(buf.data()), hd.regPoolSize);
+    }
+    for (uint32_t st = 0; st < n; ++st)
+      for (uint64_t off = 0; off < hd.memPoolSize; off += buf.size()) {
+        const size_t len = size_t(std::min<uint64_t>(buf.size(), hd.memPoolSize - off));
+        TGS_CUDA(cudaMemcpy(buf.data(), h->mems.p + size_t(st) * h->memStride + off, len, cudaMemcpyDeviceToHost));
+        o.write(reinterpret_cast<const char *>(buf.data()), std::streamsize(len));
+      }
+    if (!o) throw Error(TGS_ERR_IO, std::string("write failed: ") + path);
+  });
+}
+
+int tgs_load_state(tgs_sim *h, const char *path) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!path) throw Error(TGS_ERR_ARG, "null path");
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw Error(TGS_ERR_IO, std::string("cannot read ") + path);
+    StateHeader hd{};
+    in.read(reinterpret_cast<char *>(&hd), sizeof(hd));
+    if (!in || std::memcmp(hd.magic, kStateMagic, 8) != 0 || hd.version != kStateVersion)
+      throw Error(TGS_ERR_FORMAT, std::string("not a state file: ") + path);
+    if (hd.fingerprint != designFingerprint(h->design) || hd.regPoolSize != h->design.regPoolSize ||
+        hd.memPoolSize != h->design.memPoolSize)
+      throw Error(TGS_ERR_ARG, "state file of another design");
+    if (hd.nStreams == 0) throw Error(TGS_ERR_FORMAT, "state file without streams");
+    const uint32_t n = hd.nStreams;
+    std::vector<uint32_t> stop(n), stopCycle(n);
+    std::vector<unsigned long long> roll(n);
+    in.read(reinterpret_cast<char *>(stop.data()), n * 4ull);
+    in.read(reinterpret_cast<char *>(stopCycle.data()), n * 4ull);
+    in.read(reinterpret_cast<char *>(roll.data()), n * 8ull);
+    if (!in) throw Error(TGS_ERR_FORMAT, "truncated state file");
+    if (h->opt.n_streams != n) {
+      h->opt.n_streams = n;
+      configure(h);
+    }
+    resetState(h);  // padding slots and words take their initial values
+    h->ioBytes.alloc(std::max<size_t>(h->ioBytes.n, h->regSlots));
+    std::vector<uint8_t> buf(std::max<size_t>(h->regSlots, size_t(1) << 24));
+    for (uint32_t st = 0; st < n; ++st) {
+      uint32_t g, k;
+      streamPos(h, st, g, k);
+      in.read(reinterpret_cast<char *>(buf.data()), hd.regPoolSize);
+      if (!in) throw Error(TGS_ERR_FORMAT, "truncated state file");
+      // padding slots past regPoolSize keep their current (initial) values
+      TGS_CUDA(launchGatherRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+      TGS_CUDA(cudaMemcpyAsync(buf.data() + hd.regPoolSize, h->ioBytes.p + hd.regPoolSize,
+                               h->regSlots - hd.regPoolSize, cudaMemcpyDeviceToHost, h->stream));
+      TGS_CUDA(cudaStreamSynchronize(h->stream));
+      TGS_CUDA(cudaMemcpyAsync(h->ioBytes.p, buf.data(), h->regSlots, cudaMemcpyHostToDevice, h->stream));
+      TGS_CUDA(launchScatterRegs(h->regs.p, h->regSlots, h->gpad, g, k, h->ioBytes.p, h->stream));
+      TGS_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    for (uint32_t st = 0; st < n; ++st)
+      for (uint64_t off = 0; off < hd.memPoolSize; off += buf.size()) {
+        const size_t len = size_t(std::min<uint64_t>(buf.size(), hd.memPoolSize - off));
+        in.read(reinterpret_cast<char *>(buf.data()), std::streamsize(len));
+        if (!in) throw Error(TGS_ERR_FORMAT, "truncated state file");
+        TGS_CUDA(cudaMemcpy(h->mems.p + size_t(st) * h->memStride + off, buf.data(), len, cudaMemcpyHostToDevice));
+      }
+    TGS_CUDA(cudaMemcpy(h->stop.p, stop.data(), n * 4ull, cudaMemcpyHostToDevice));
+    TGS_CUDA(cudaMemcpy(h->stopCycle.p, stopCycle.data(), n * 4ull, cudaMemcpyHostToDevice));
+    TGS_CUDA(cudaMemcpy(h->roll.p, roll.data(), n * 8ull, cudaMemcpyHostToDevice));
+    TGS_CUDA(cudaMemcpy(h->realCycles.p, &hd.realCycles, 4, cudaMemcpyHostToDevice));
+    h->cycleCnt = hd.cycleCnt;
+    h->batchCycle = hd.batchCycle;
   });
 }
 
@@ -1125,6 +1299,7 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   }
   const bool wantDigest = (job->flags & (TGS_BATCH_CYCLE_DIGESTS | TGS_BATCH_ROLLING)) != 0;
   if (wantDigest) flags |= kFlagDigest;
+  if (job->flags & TGS_BATCH_STOP_EXIT) flags |= kFlagStopExit;
   if (flags) checkRegionRoles(h);
   if (flags & kFlagStimulus) {
     h->stimReg.upload(st->reg, st->n_inputs, h->stream);
@@ -1136,6 +1311,7 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   const bool admission = !equal || (job->slots && job->slots < n);
   if (admission) {
     if (job->flags & TGS_BATCH_CONTINUE) throw Error(TGS_ERR_ARG, "TGS_BATCH_CONTINUE needs every stream resident");
+    if (job->flags & TGS_BATCH_STOP_EXIT) throw Error(TGS_ERR_ARG, "TGS_BATCH_STOP_EXIT needs every stream resident");
     fillParams(h);  // refreshed below after any reconfiguration
     batchAdmission(h, job, res, flags);
     return;
@@ -1185,6 +1361,14 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   if (!res) return;
   res->device_ms = ms;
   res->stream_cycles = uint64_t(cyc) * n;
+  if (flags & kFlagStopExit) {
+    // a stream that stopped ran up to and including its stop cycle
+    std::vector<uint32_t> sc(n);
+    TGS_CUDA(cudaMemcpy(sc.data(), h->stopCycle.p, n * 4ull, cudaMemcpyDeviceToHost));
+    res->stream_cycles = 0;
+    for (uint32_t q = 0; q < n; ++q)
+      res->stream_cycles += sc[q] == 0xFFFFFFFFu ? cyc : (sc[q] >= c0 ? sc[q] + 1 - c0 : 0);
+  }
   res->launches = h->lastLaunches;
   cudaStream_t s = h->stream;
   if (res->final_reg_digest || res->final_mem_digest) {

@@ -84,6 +84,13 @@ class Simulator:
         check(lib().tgs_eval_free_running(self._h, int(max_cycles), C.byref(stop)))
         return bool(stop.value)
 
+    def eval_until_stop(self, max_cycles: int) -> tuple[bool, int]:
+        """Free running that ends once every stream executed a stop op
+        (stopped streams freeze).  Returns (stop flag, cycles run)."""
+        stop, ran = C.c_int(), C.c_uint32()
+        check(lib().tgs_eval_until_stop(self._h, int(max_cycles), C.byref(stop), C.byref(ran)))
+        return bool(stop.value), ran.value
+
     def set_register(self, name: str, value: int, stream: int = 0) -> None:
         check(lib().tgs_set_register_stream(self._h, stream, name.encode(), int(value)))
 
@@ -177,10 +184,19 @@ class Simulator:
     def reset_state(self) -> None:
         check(lib().tgs_reset_state(self._h))
 
+    def dump_state(self, path) -> None:
+        """Checkpoint every stream's state and the cycle counters to a file."""
+        check(lib().tgs_dump_state(self._h, str(path).encode()))
+
+    def load_state(self, path) -> None:
+        """Restore a checkpoint of the same design (takes its stream count)."""
+        check(lib().tgs_load_state(self._h, str(path).encode()))
+        check(lib().tgs_get_options(self._h, C.byref(self._opt)))
+
     # -- batched runs ---------------------------------------------------------
     def batch_run(self, cycles, stim: "StimulusSpec | None" = None, *, cycle_digests: bool = False,
                   rolling: bool = True, final_state: bool = False, slots: int = 0, continue_: bool = False,
-                  final_digests: bool = True) -> "BatchOutput":
+                  final_digests: bool = True, stop_exit: bool = False) -> "BatchOutput":
         cyc = np.ascontiguousarray(cycles, np.uint32)
         n = int(cyc.size)
         out = BatchOutput(n)
@@ -192,7 +208,8 @@ class Simulator:
             out.final_regs = np.zeros((n, r), np.uint8)
             out.final_mems = np.zeros((n, m), np.uint8)
         flags = (capi.BATCH_CYCLE_DIGESTS if cycle_digests else 0) | (capi.BATCH_ROLLING if rolling else 0) | (
-            capi.BATCH_FINAL_STATE if final_state else 0) | (capi.BATCH_CONTINUE if continue_ else 0)
+            capi.BATCH_FINAL_STATE if final_state else 0) | (capi.BATCH_CONTINUE if continue_ else 0) | (
+            capi.BATCH_STOP_EXIT if stop_exit else 0)
         st_ptr = C.cast(None, C.POINTER(capi.Stimulus))
         keep = []
         if stim is not None:
@@ -304,13 +321,20 @@ def mix64(z: np.ndarray) -> np.ndarray:
         return z ^ (z >> np.uint64(31))
 
 
-def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out: np.ndarray | None = None) -> np.ndarray:
+def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out: np.ndarray | None = None,
+                   prev: np.ndarray | None = None) -> np.ndarray:
     """The seeded input values of cycles [c0, c0 + cycles) as a host table
-    [cycle][input][stream] (uniform inputs only), identical to what the
-    device computes from the seed."""
-    if spec.toggle is not None and np.any(spec.toggle):
-        raise ValueError("toggle inputs depend on the previous value; tables hold uniform inputs")
+    [cycle][input][stream] of nibble values, identical to what the device
+    computes from the seed.  Toggle inputs flip the previous value: `prev`
+    [input][stream] holds the values before cycle c0 (the initial register
+    nibbles for c0 = 0, else the last row of the previous table)."""
     n_in = len(spec.reg)
+    tog = None
+    if spec.toggle is not None and np.any(spec.toggle):
+        if prev is None:
+            raise ValueError("toggle inputs need the values before cycle c0 (prev)")
+        tog = np.asarray(spec.toggle, np.uint64)
+        cur = np.array(prev, np.uint8).reshape(n_in, n_streams).copy()
     seeds = mix64(np.uint64(spec.base_seed) ^ np.arange(n_streams, dtype=np.uint64))
     masks = ((np.uint32(1) << np.asarray(spec.bits, np.uint32)) - 1).astype(np.uint64)
     if out is None:
@@ -319,7 +343,14 @@ def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out
     for c in range(cycles):
         key = mix64((np.uint64(c0 + c) << np.uint64(32)) | inp)           # [n_in]
         h = mix64(seeds[None, :] ^ key[:, None])                          # [n_in, n_streams]
-        out[c] = (h & masks[:, None]).astype(np.uint8)
+        uni = (h & masks[:, None]).astype(np.uint8)
+        if tog is None:
+            out[c] = uni
+        else:
+            flip = (h >> np.uint64(48)) < tog[:, None]
+            toggled = np.where(flip, cur ^ masks[:, None].astype(np.uint8), cur)
+            cur = np.where(tog[:, None] == 0, uni, toggled).astype(np.uint8)
+            out[c] = cur
     return out
 
 
