@@ -197,9 +197,14 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
   }
 }
 
+// Special micro-partitions run on the stream groups [g0, g0 + gn) of the
+// item: the schedule may give the groups of one micro-partition to several
+// warps (a level of one special micro-partition would leave the other warps
+// idle).
 template <int SPW, int G>
 __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp,
-                                            uint32_t hdr, uint32_t *__restrict__ vp, uint32_t lane) {
+                                            uint32_t hdr, uint32_t *__restrict__ vp, uint32_t lane, uint32_t g0,
+                                            uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
   const uint32_t *r = mp + kMPHeaderWords + lane * kVecReadWords;
@@ -209,7 +214,7 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
   const uint32_t outR = w4 & 0xFFFFu, res = w4 >> 16;
   const uint8_t *cv = p.constVec + d.constOff;
 #pragma unroll 1
-  for (int g = 0; g < G; ++g) {
+  for (uint32_t g = g0; g < g0 + gn; ++g) {
     uint32_t I[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : vp[ix[j] * G + g];
@@ -231,60 +236,70 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
 
 // Signed vector arithmetic on up to 31 nibbles per stream (SimEval.cu:482-548):
 // nibble i of the vector sits in slot base + i, sign bit at 4 * len - 1.
+// Work item = (op, group, stream), one per lane: the SPW lanes of one (op,
+// group) hold the streams of one word and merge their result nibbles with
+// shuffles, so no lane runs the streams of a word one after another.
 template <int SPW, int G>
 __device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp, uint32_t hdr,
-                          uint32_t *__restrict__ vp, uint32_t lane) {
+                          uint32_t *__restrict__ vp, uint32_t lane, uint32_t g0, uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
-  if (lane >= n) return;
-  const uint32_t *r = mp + kMPHeaderWords + lane * kVecOpWords;
-  const uint32_t w0 = r[0], w1 = r[1], res = r[2];
-  const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = w1 & 0xFFFFu, op = (w1 >> 16) & 0xFFu, cf = w1 >> 24;
-  const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
+  const uint32_t total = n * gn * SPW;
   const uint8_t *cv = p.constVec + d.constOff;
-  const bool isVec = op <= 2;
-  const uint32_t sign = 4 * len - 1;
 #pragma unroll 1
-  for (int g = 0; g < G; ++g) {
-#pragma unroll 1
-    for (int k = 0; k < SPW; ++k) {
-      unsigned __int128 a = 0, b = 0;
-      for (uint32_t i = 0; i < len; ++i) {
-        const uint32_t x = c1 ? (uint32_t(cv[v1 + i]) & 15u) : nib(vp[(v1 + i) * G + g], k);
-        const uint32_t y = c2 ? (uint32_t(cv[v2 + i]) & 15u) : nib(vp[(v2 + i) * G + g], k);
-        a |= (unsigned __int128)x << (4 * i);
-        b |= (unsigned __int128)y << (4 * i);
-      }
+  for (uint32_t base = 0; base < total; base += 32) {  // the same trip count in every lane
+    const uint32_t w = base + lane;
+    const bool act = w < total;
+    const uint32_t op = act ? w / (gn * SPW) : 0u;
+    const uint32_t g = g0 + (w / SPW) % gn, k = w % SPW;
+    const uint32_t *r = mp + kMPHeaderWords + op * kVecOpWords;
+    const uint32_t w0 = r[0], w1 = r[1], res = r[2];
+    const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = act ? (w1 & 0xFFFFu) : 0u, opc = (w1 >> 16) & 0xFFu;
+    const uint32_t cf = w1 >> 24;
+    const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
+    const bool isVec = opc <= 2;
+    unsigned __int128 a = 0, b = 0;
+    for (uint32_t i = 0; i < len; ++i) {
+      const uint32_t x = c1 ? (uint32_t(cv[v1 + i]) & 15u) : nib(vp[(v1 + i) * G + g], k);
+      const uint32_t y = c2 ? (uint32_t(cv[v2 + i]) & 15u) : nib(vp[(v2 + i) * G + g], k);
+      a |= (unsigned __int128)x << (4 * i);
+      b |= (unsigned __int128)y << (4 * i);
+    }
+    unsigned __int128 rv = 0;
+    if (act) {
+      const uint32_t sign = 4 * len - 1;
       if ((a >> sign) & 1) a |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
       if ((b >> sign) & 1) b |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
       const __int128 sa = (__int128)a, sb = (__int128)b;
-      unsigned __int128 rv = 0;
-      uint32_t bit = 0;
-      switch (op) {
+      switch (opc) {
         case 0: rv = a + b; break;
         case 1: rv = a - b; break;
         case 2: rv = a * b; break;
-        case 3: bit = sa == sb; break;
-        case 4: bit = sa < sb; break;
-        case 5: bit = sa <= sb; break;
-        default: bit = 0; break;
+        case 3: rv = sa == sb; break;
+        case 4: rv = sa < sb; break;
+        case 5: rv = sa <= sb; break;
+        default: rv = 0; break;
       }
-      const uint32_t kmask = ~(15u << (4 * k));
-      if (isVec) {
-        for (uint32_t i = 0; i < len; ++i) {
-          const uint32_t s = (res + i) & 0xFFFFu;
-          const uint32_t nv = uint32_t(rv >> (4 * i)) & 15u;
-          vp[s * G + g] = (k == 0 ? 0u : (vp[s * G + g] & kmask)) | (nv << (4 * k));
-        }
-      } else {
-        vp[res * G + g] = (k == 0 ? 0u : (vp[res * G + g] & kmask)) | (bit << (4 * k));
-      }
+    }
+    // result nibbles: len slots for arithmetic, one slot for a comparison
+    const uint32_t outLen = act ? (isVec ? len : 1u) : 0u;
+    uint32_t maxLen = outLen;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxLen = max(maxLen, __shfl_xor_sync(kFull, maxLen, o));
+    for (uint32_t i = 0; i < maxLen; ++i) {
+      uint32_t word = i < outLen ? (uint32_t(rv >> (4 * i)) & 15u) << (4 * k) : 0u;
+#pragma unroll
+      for (int o = 1; o < SPW; o <<= 1) word |= __shfl_xor_sync(kFull, word, o);
+      if (k == 0 && i < outLen) vp[((res + i) & 0xFFFFu) * G + g] = word;
     }
   }
 }
 
+// Memory reads (SimEval.cu:550-575): the loads of the SPW streams of a word
+// are issued together, then merged.
 template <int SPW, int G>
 __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__restrict__ mp, uint32_t hdr,
-                                            uint32_t *__restrict__ vp, uint32_t lane, uint32_t gb) {
+                                            uint32_t *__restrict__ vp, uint32_t lane, uint32_t gb, uint32_t g0,
+                                            uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
   const uint32_t *r = mp + kMPHeaderWords + lane * kMemReadWords;
@@ -294,15 +309,17 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
   const uint32_t en = w2 & 0xFFFFu, av = w2 >> 16;
   if (en == 0) return;  // immediate 0: neither reads nor writes (SimEval.cu:559-560)
 #pragma unroll 1
-  for (int g = 0; g < G; ++g) {
+  for (uint32_t g = g0; g < g0 + gn; ++g) {
     const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
     uint32_t AD[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) AD[j] = vp[(av + j) * G + g];
     uint32_t out = vp[res * G + g];  // a disabled read leaves the slot as it is
+    uint32_t val[SPW];
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
       const uint32_t s = (gb * G + g) * SPW + k;
+      val[k] = 16u;  // no load
       if (s >= p.nStreams || nib(EN, k) == 0) continue;
       uint32_t addr = 0;
 #pragma unroll
@@ -313,9 +330,11 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
         raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
         continue;
       }
-      const uint32_t val = __ldcg(p.mems + s * p.memStride + idx) & 15u;
-      out = (out & ~(15u << (4 * k))) | (val << (4 * k));
+      val[k] = __ldcg(p.mems + s * p.memStride + idx) & 15u;
     }
+#pragma unroll
+    for (int k = 0; k < SPW; ++k)
+      if (val[k] < 16u) out = (out & ~(15u << (4 * k))) | (val[k] << (4 * k));
     vp[res * G + g] = out;
   }
 }
@@ -412,20 +431,23 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     const uint32_t *units = blk + 2 + NW;
     const bool profileMP = (p.flags & kFlagProfileMP) != 0;
     for (uint32_t u = ub; u < ue; ++u) {
-      const uint32_t *mp = blk + units[u];
+      // unit word: record offset | first group << 26 | (groups - 1) << 28
+      const uint32_t uw = units[u];
+      const uint32_t *mp = blk + (uw & kUnitOffsetMask);
+      const uint32_t g0 = (uw >> 26) & 3u, gn = ((uw >> 28) & 3u) + 1u;
       const uint32_t hdr = mp[0];
       const long long tm = profileMP ? clock64() : 0;
       switch (hdr & 3u) {
-        case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;
-        case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane); break;
-        case kMPVecOp: evalVecOp<SPW, G>(p, d, mp, hdr, vp, lane); break;
-        default: evalMemRead<SPW, G>(p, mp, hdr, vp, lane, gb); break;
+        case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;  // always every group
+        case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane, g0, gn); break;
+        case kMPVecOp: evalVecOp<SPW, G>(p, d, mp, hdr, vp, lane, g0, gn); break;
+        default: evalMemRead<SPW, G>(p, mp, hdr, vp, lane, gb, g0, gn); break;
       }
       __syncwarp();
       if (profileMP && lane == 0) {
         const uint32_t id = mp[1];
         atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
-        atomicAdd(p.mpCount + id, 1u);
+        atomicAdd(p.mpCount + id, gn);  // groups evaluated
       }
     }
   }

@@ -33,6 +33,9 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 //   MemRead (4 words): memBase lo, memBase hi | multiWriter << 31, en | addrVec << 16, result
 constexpr uint32_t kMPHeaderWords = 4;
 constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;
+// schedule unit word: record offset (words from the level block) | first
+// group << 26 | (groups - 1) << 28
+constexpr uint32_t kUnitOffsetMask = (1u << 26) - 1u;
 
 struct PartDesc {
   uint32_t vpSlots;      // value-pool slots (multiple of 4)
@@ -56,8 +59,9 @@ static_assert(sizeof(PartDesc) == 96, "PartDesc size");
 
 // Exec levels (KParams::sched), for NW warps: one 16-byte aligned block per
 // partition level, [flags (bit0: block barrier)][NW + 1 prefix offsets into
-// the unit list][unit list: word offsets of the micro-partitions relative to
-// the block][micro-partition records in warp order].  KParams::levelDesc
+// the unit list][unit list: unit words (kUnitOffsetMask), each a record
+// offset relative to the block and a range of stream groups][micro-partition
+// records, once each, in warp order].  KParams::levelDesc
 // holds (block offset, block words) per level; PartDesc::schedOff indexes
 // the partition's first level there.  A block is staged into shared memory
 // with one bulk async copy while the previous level computes.

@@ -296,8 +296,9 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots) {
 // Greedy gate-count cost of a micro-partition (the fallback cost model).
 float gateCost(const MPartFeat &f) { return float(std::max<uint32_t>(1, f.ops)); }
 
-void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const std::vector<std::vector<std::vector<float>>> *cost,
-                   uint32_t nBlocks, uint32_t nGroupBlocks, Schedule &out) {
+void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,
+                   const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,
+                   Schedule &out) {
   out = Schedule();
   out.NW = NW;
   out.partCost.assign(d.parts.size(), 0.0);
@@ -312,24 +313,39 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
     std::vector<uint32_t> touched;
     for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
       const auto &mps = img.mp[pid][lv];
-      // LPT: largest cost first onto the least loaded warp
-      std::vector<uint32_t> order(mps.size());
-      std::iota(order.begin(), order.end(), 0u);
       auto costOf = [&](uint32_t i) { return cost ? (*cost)[pid][lv][i] : gateCost(mps[i].feat); };
-      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return costOf(a) > costOf(b); });
+      // units: a LUT micro-partition runs every group of the item in one warp
+      // (its lanes share the operand loads); a special one is split into one
+      // unit per group, so a level holding one of them keeps G warps busy
+      struct Unit {
+        uint32_t i, g0, gn;
+        double c;
+      };
+      std::vector<Unit> units;
+      for (uint32_t i = 0; i < mps.size(); ++i) {
+        if (mps[i].feat.kind != kMPLut && G > 1)
+          for (uint32_t g = 0; g < G; ++g) units.push_back({i, g, 1, costOf(i) / G});
+        else
+          units.push_back({i, 0, G, costOf(i)});
+      }
+      // LPT: largest cost first onto the least loaded warp
+      std::vector<uint32_t> order(units.size());
+      std::iota(order.begin(), order.end(), 0u);
+      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return units[a].c > units[b].c; });
       std::vector<double> load(NW, 0.0);
-      std::vector<std::vector<uint32_t>> perWarp(NW);
-      for (uint32_t i : order) {
+      std::vector<std::vector<uint32_t>> perWarp(NW);  // unit indices
+      for (uint32_t u : order) {
         uint32_t w = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
-        load[w] += costOf(i);
-        perWarp[w].push_back(i);
+        load[w] += units[u].c;
+        perWarp[w].push_back(u);
       }
       total += *std::max_element(load.begin(), load.end());
       // does this level need a block barrier first?
       bool need = lv == 0;
       if (!need) {
         for (uint32_t w = 0; w < NW && !need; ++w)
-          for (uint32_t i : perWarp[w]) {
+          for (uint32_t u : perWarp[w]) {
+            const uint32_t i = units[u].i;
             for (uint32_t s : mps[i].reads)
               if (lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) { need = true; break; }
             if (need) break;
@@ -343,10 +359,18 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
         touched.clear();
         out.barriers++;
       }
+      // a slot written by units of one micro-partition on several warps
+      // counts as written by each of them (the last one recorded): every
+      // later access from another warp then needs a barrier
       for (uint32_t w = 0; w < NW; ++w)
-        for (uint32_t i : perWarp[w]) {
+        for (uint32_t u : perWarp[w]) {
+          const uint32_t i = units[u].i;
           for (uint32_t s : mps[i].reads) { readersMask[s] |= 1u << w; touched.push_back(s); }
-          for (uint32_t s : mps[i].writes) { lastWriter[s] = int32_t(w); touched.push_back(s); }
+          for (uint32_t s : mps[i].writes) {
+            if (lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) lastWriter[s] = int32_t(NW);  // several warps
+            else lastWriter[s] = int32_t(w);
+            touched.push_back(s);
+          }
         }
       out.levels++;
       // level block: [flags][NW + 1 prefix offsets][unit offsets][pad][micro-partitions in warp order]
@@ -365,12 +389,18 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, const 
       sw.resize(sw.size() + nUnits, 0);
       while (sw.size() % 4) sw.push_back(0);
       uint32_t u = 0;
+      std::vector<uint32_t> recordAt(mps.size(), UINT32_MAX);  // one record per micro-partition
       for (uint32_t w = 0; w < NW; ++w)
-        for (uint32_t i : perWarp[w]) {
-          sw[unitBase + u++] = uint32_t(sw.size()) - blk;
-          const MPartRef &r = mps[i];
-          sw.insert(sw.end(), img.net.begin() + r.off, img.net.begin() + r.off + r.words);
-          while (sw.size() % 4) sw.push_back(0);
+        for (uint32_t x : perWarp[w]) {
+          const Unit &un = units[x];
+          if (recordAt[un.i] == UINT32_MAX) {
+            recordAt[un.i] = uint32_t(sw.size()) - blk;
+            const MPartRef &r = mps[un.i];
+            sw.insert(sw.end(), img.net.begin() + r.off, img.net.begin() + r.off + r.words);
+            while (sw.size() % 4) sw.push_back(0);
+          }
+          if (recordAt[un.i] > kUnitOffsetMask) throw Error(TGS_ERR_RESOURCES, "exec level too large");
+          sw[unitBase + u++] = recordAt[un.i] | (un.g0 << 26) | ((un.gn - 1) << 28);
         }
       const uint32_t words = uint32_t(sw.size()) - blk;
       out.levelDesc.push_back(blk);

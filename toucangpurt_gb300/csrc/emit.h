@@ -63,7 +63,8 @@ struct Schedule {
 // compactSlots: renumber value-pool slots by live range (slotalloc.h)
 void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
-void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW,
+// G: stream groups per item (special micro-partitions are split by group).
+void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,
                    const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,
                    Schedule &out);
 float gateCost(const MPartFeat &f);

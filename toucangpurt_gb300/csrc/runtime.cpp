@@ -260,7 +260,7 @@ void configure(tgs_sim *h) {
                                        " groups needs " + std::to_string(kLutTablePadded + vpBytes) +
                                        " B of shared memory; lower groups_per_item");
   // first pass to learn the largest level block (independent of the block count)
-  buildSchedule(h->design, h->img, NW, costPtr, 1, nGB, h->sched);
+  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, 1, nGB, h->sched);
   uint32_t stage = o.resident_netlist == 2 ? 0u : std::min<uint32_t>(h->sched.maxLevelWords, 4096u);
   int perSM = shape(stage);
   const int perSMNoStage = shape(0);
@@ -279,7 +279,7 @@ void configure(tgs_sim *h) {
   if (perSM <= 0) throw Error(TGS_ERR_RESOURCES, "no block of the cycle kernel fits on an SM with this configuration");
   h->stageWords = stage;
   h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
-  buildSchedule(h->design, h->img, NW, costPtr, h->lc.blocks, nGB, h->sched);
+  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, h->lc.blocks, nGB, h->sched);
   h->parts.upload(h->img.parts, h->stream);
   h->schedW.upload(h->sched.words, h->stream);
   h->levelDesc.upload(h->sched.levelDesc, h->stream);
@@ -1587,7 +1587,9 @@ extern "C" int tgs_profile_mparts(tgs_sim *h, uint32_t cycles, float *mean_cycle
     std::vector<uint32_t> k(n);
     TGS_CUDA(cudaMemcpy(c.data(), h->mpCycles.p, size_t(n) * 8, cudaMemcpyDeviceToHost));
     TGS_CUDA(cudaMemcpy(k.data(), h->mpCount.p, size_t(n) * 4, cudaMemcpyDeviceToHost));
-    for (uint32_t i = 0; i < n; ++i) mean_cycles[i] = k[i] ? float(double(c[i]) / k[i]) : 0.f;
+    // counts are groups evaluated: a whole evaluation covers G of them
+    const double G = double(h->lc.G);
+    for (uint32_t i = 0; i < n; ++i) mean_cycles[i] = k[i] ? float(double(c[i]) * G / k[i]) : 0.f;
     fillParams(h);
   });
 }
