@@ -57,104 +57,176 @@ __device__ __forceinline__ void raiseErr(const KParams &p, uint32_t code, uint32
   }
 }
 
+// ---- shared memory -----------------------------------------------------------
+// Every shared-memory access of the evaluation goes through these helpers with
+// 32-bit shared-window addresses, so the compiler emits shared loads and
+// stores.  (A pointer that may refer to shared or to global memory, such as
+// an exec level that is staged or not, would otherwise compile to generic
+// accesses with 64-bit address arithmetic.)  Stores carry a memory clobber;
+// loads are volatile, so the compiler keeps them in order with the stores.
+__device__ __forceinline__ uint32_t ldsU8(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint32_t ldsU32(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint2 ldsV2(uint32_t a) {
+  uint2 v;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint4 ldsV4(uint32_t a) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void stsU32(uint32_t a, uint32_t v) {
+  asm volatile("st.shared.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void stsV2(uint32_t a, uint2 v) {
+  asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
+}
+__device__ __forceinline__ void stsV4(uint32_t a, uint4 v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
+}
+
+// Words of a level block / micro-partition record: staged in shared memory
+// (SH) or read from the schedule in global memory.
+template <bool SH>
+struct Words {
+  const uint32_t *g;  // global address (SH = false)
+  uint32_t s;         // shared address (SH = true)
+  __device__ __forceinline__ uint32_t operator[](uint32_t i) const {
+    if constexpr (SH) return ldsU32(s + 4u * i);
+    else return __ldg(g + i);
+  }
+  // words i, i + 1 (i even: records are 16-byte aligned)
+  __device__ __forceinline__ uint2 pair(uint32_t i) const {
+    if constexpr (SH) return ldsV2(s + 4u * i);
+    else return __ldg(reinterpret_cast<const uint2 *>(g + i));
+  }
+  __device__ __forceinline__ Words at(uint32_t off) const { return Words{g + off, s + 4u * off}; }
+};
+
+// value-pool slot word (slot, group) of a block's pool at shared address vp
+template <int G>
+__device__ __forceinline__ uint32_t vpAddr(uint32_t vp, uint32_t slot, uint32_t g) {
+  return vp + 4u * (slot * uint32_t(G) + g);
+}
+
 // ---- truth-table lookup ---------------------------------------------------
-// index = lutIndex + (a << 8 | b << 4 | c) per stream (SimEval.cu:353,410).
+// index = lutIndex + (a << 8 | b << 4 | c) per stream (SimEval.cu:353,410);
+// tab = shared address of the staged table.
 template <int SPW>
-__device__ __forceinline__ uint32_t lookup(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
-                                           uint32_t C);
+__device__ __forceinline__ uint32_t lookup(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C);
 
 template <>
-__device__ __forceinline__ uint32_t lookup<1>(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
-                                              uint32_t C) {
-  return tab[base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u))];
+__device__ __forceinline__ uint32_t lookup<1>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
+  return ldsU8(tab + base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
 }
 
 // 8 streams: even streams sit in the low nibble of each byte, odd streams in
 // the high nibble.  (b << 4 | c) of 4 streams is formed per byte lane with
 // masks, the a nibble is paired with it by byte permutes into two 12-bit
-// indices per word, and the 8 table bytes are packed back with shifts.
+// indices per word, and the 8 table bytes are packed back with permutes.
 template <>
-__device__ __forceinline__ uint32_t lookup<8>(const uint8_t *__restrict__ tab, uint32_t base, uint32_t A, uint32_t B,
-                                              uint32_t C) {
-  const uint8_t *t = tab + base;
+__device__ __forceinline__ uint32_t lookup<8>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
+  const uint32_t t = tab + base;
   const uint32_t bcE = ((B & 0x0F0F0F0Fu) << 4) | (C & 0x0F0F0F0Fu);
   const uint32_t bcO = (B & 0xF0F0F0F0u) | ((C >> 4) & 0x0F0F0F0Fu);
   const uint32_t aE = A & 0x0F0F0F0Fu, aO = (A >> 4) & 0x0F0F0F0Fu;
   const uint32_t e01 = __byte_perm(bcE, aE, 0x5140), e23 = __byte_perm(bcE, aE, 0x7362);
   const uint32_t o01 = __byte_perm(bcO, aO, 0x5140), o23 = __byte_perm(bcO, aO, 0x7362);
-  const uint32_t r0 = t[e01 & 0xFFFFu], r2 = t[e01 >> 16], r4 = t[e23 & 0xFFFFu], r6 = t[e23 >> 16];
-  const uint32_t r1 = t[o01 & 0xFFFFu], r3 = t[o01 >> 16], r5 = t[o23 & 0xFFFFu], r7 = t[o23 >> 16];
-  const uint32_t lo = r0 | (r2 << 8) | (r4 << 16) | (r6 << 24);
-  const uint32_t hi = r1 | (r3 << 8) | (r5 << 16) | (r7 << 24);
+  const uint32_t r0 = ldsU8(t + (e01 & 0xFFFFu)), r2 = ldsU8(t + (e01 >> 16));
+  const uint32_t r4 = ldsU8(t + (e23 & 0xFFFFu)), r6 = ldsU8(t + (e23 >> 16));
+  const uint32_t r1 = ldsU8(t + (o01 & 0xFFFFu)), r3 = ldsU8(t + (o01 >> 16));
+  const uint32_t r5 = ldsU8(t + (o23 & 0xFFFFu)), r7 = ldsU8(t + (o23 >> 16));
+  const uint32_t lo = __byte_perm(__byte_perm(r0, r2, 0x0040), __byte_perm(r4, r6, 0x0040), 0x5410);
+  const uint32_t hi = __byte_perm(__byte_perm(r1, r3, 0x0040), __byte_perm(r5, r7, 0x0040), 0x5410);
   return lo | (hi << 4);
 }
 
 // ---- value-pool words of G groups ----------------------------------------
 template <int G>
-__device__ __forceinline__ void loadG(const uint32_t *__restrict__ src, uint32_t (&v)[G]) {
+__device__ __forceinline__ void loadG(uint32_t sa, uint32_t (&v)[G]) {
   if constexpr (G == 4) {
-    const uint4 q = *reinterpret_cast<const uint4 *>(src);
+    const uint4 q = ldsV4(sa);
     v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
   } else if constexpr (G == 2) {
-    const uint2 q = *reinterpret_cast<const uint2 *>(src);
+    const uint2 q = ldsV2(sa);
     v[0] = q.x; v[1] = q.y;
   } else {
-    v[0] = *src;
-  }
-}
-
-// global (mutable state, L1 bypass) -> shared
-template <int G>
-__device__ __forceinline__ void copyInG(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src) {
-  if constexpr (G == 4) {
-    *reinterpret_cast<uint4 *>(dst) = __ldcg(reinterpret_cast<const uint4 *>(src));
-  } else if constexpr (G == 2) {
-    *reinterpret_cast<uint2 *>(dst) = __ldcg(reinterpret_cast<const uint2 *>(src));
-  } else {
-    *dst = __ldcg(src);
+    v[0] = ldsU32(sa);
   }
 }
 
 template <int G>
-__device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src) {
+__device__ __forceinline__ void storeG(uint32_t sa, const uint32_t (&v)[G]) {
   if constexpr (G == 4) {
-    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(src);
+    stsV4(sa, make_uint4(v[0], v[1], v[2], v[3]));
   } else if constexpr (G == 2) {
-    *reinterpret_cast<uint2 *>(dst) = *reinterpret_cast<const uint2 *>(src);
+    stsV2(sa, make_uint2(v[0], v[1]));
   } else {
-    *dst = *src;
+    stsU32(sa, v[0]);
+  }
+}
+
+// global (mutable state, L1 bypass) -> value pool
+template <int G>
+__device__ __forceinline__ void copyInG(uint32_t dst, const uint32_t *__restrict__ src) {
+  if constexpr (G == 4) {
+    stsV4(dst, __ldcg(reinterpret_cast<const uint4 *>(src)));
+  } else if constexpr (G == 2) {
+    stsV2(dst, __ldcg(reinterpret_cast<const uint2 *>(src)));
+  } else {
+    stsU32(dst, __ldcg(src));
+  }
+}
+
+// value pool -> global
+template <int G>
+__device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t src) {
+  if constexpr (G == 4) {
+    *reinterpret_cast<uint4 *>(dst) = ldsV4(src);
+  } else if constexpr (G == 2) {
+    *reinterpret_cast<uint2 *>(dst) = ldsV2(src);
+  } else {
+    *dst = ldsU32(src);
   }
 }
 
 // ---- micro-partitions (evalSingleMicroPart, SimEval.cu:304-580) -----------
-template <int SPW, int G>
-__device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_t hdr, uint32_t *__restrict__ vp,
-                                        const uint8_t *__restrict__ tab, uint32_t lane) {
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void evalLut(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane) {
   const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
-  const uint32_t *top = mp + kMPHeaderWords;
+  const Words<SH> top = mp.at(kMPHeaderWords);
   uint32_t v[G];
   // top level: operands < 16 are immediates, else value-pool slots
   if (lane < W) {
-    const uint2 t = reinterpret_cast<const uint2 *>(top)[lane];
+    const uint2 t = top.pair(2u * lane);
     const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
     uint32_t A[G], B[G], C[G];
     if (a < 16) {
 #pragma unroll
       for (int g = 0; g < G; ++g) A[g] = rep8(a);
     } else {
-      loadG<G>(vp + a * G, A);
+      loadG<G>(vpAddr<G>(vp, a, 0), A);
     }
     if (b < 16) {
 #pragma unroll
       for (int g = 0; g < G; ++g) B[g] = rep8(b);
     } else {
-      loadG<G>(vp + b * G, B);
+      loadG<G>(vpAddr<G>(vp, b, 0), B);
     }
     if (c < 16) {
 #pragma unroll
       for (int g = 0; g < G; ++g) C[g] = rep8(c);
     } else {
-      loadG<G>(vp + c * G, C);
+      loadG<G>(vpAddr<G>(vp, c, 0), C);
     }
 #pragma unroll
     for (int g = 0; g < G; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
@@ -163,7 +235,7 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
     for (int g = 0; g < G; ++g) v[g] = 0;
   }
   // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
-  const uint32_t *mid = top + 2 * W;
+  const Words<SH> mid = top.at(2u * W);
   for (uint32_t m = 0; m < nMid; ++m) {
     const uint32_t w = lane < W ? mid[m * W + lane] : 0u;
     const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
@@ -182,7 +254,7 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
     for (int g = 0; g < G; ++g) v[g] = nv[g];
   }
   // write-back: shuffleId < 32 immediate, else lane (shuffleId mod 32)
-  const uint32_t *wb = mid + nMid * W;
+  const Words<SH> wb = mid.at(nMid * W);
   const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;
   uint32_t out[G];
@@ -191,23 +263,19 @@ __device__ __forceinline__ void evalLut(const uint32_t *__restrict__ mp, uint32_
     const uint32_t x = __shfl_sync(kFull, v[g], int(src & 31u));
     out[g] = src < 32 ? rep8(src) : x;
   }
-  if (lane < nWB) {
-#pragma unroll
-    for (int g = 0; g < G; ++g) vp[res * G + g] = out[g];
-  }
+  if (lane < nWB) storeG<G>(vpAddr<G>(vp, res, 0), out);
 }
 
 // Special micro-partitions run on the stream groups [g0, g0 + gn) of the
 // item: the schedule may give the groups of one micro-partition to several
 // warps (a level of one special micro-partition would leave the other warps
 // idle).
-template <int SPW, int G>
-__device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp,
-                                            uint32_t hdr, uint32_t *__restrict__ vp, uint32_t lane, uint32_t g0,
-                                            uint32_t gn) {
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d, const Words<SH> mp, uint32_t hdr,
+                                            uint32_t vp, uint32_t lane, uint32_t g0, uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
-  const uint32_t *r = mp + kMPHeaderWords + lane * kVecReadWords;
+  const Words<SH> r = mp.at(kMPHeaderWords + lane * kVecReadWords);
   const uint32_t w0 = r[0], w1 = r[1], w2 = r[2], w3 = r[3], w4 = r[4];
   const uint32_t base = w0 & 0xFFFFu, len = w0 >> 16, off = w1 & 0xFFFFu, isConst = (w1 >> 16) & 1u;
   const uint32_t ix[4] = {w2 & 0xFFFFu, w2 >> 16, w3 & 0xFFFFu, w3 >> 16};
@@ -217,20 +285,20 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
   for (uint32_t g = g0; g < g0 + gn; ++g) {
     uint32_t I[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : vp[ix[j] * G + g];
-    const uint32_t OR = outR < 16 ? rep8(outR) : vp[outR * G + g];
+    for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : ldsU32(vpAddr<G>(vp, ix[j], g));
+    const uint32_t OR = outR < 16 ? rep8(outR) : ldsU32(vpAddr<G>(vp, outR, g));
     uint32_t out = 0;
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
       const uint32_t o = ((nib(I[0], k) << 12) | (nib(I[1], k) << 8) | (nib(I[2], k) << 4) | nib(I[3], k)) + off;
       uint32_t val;
       if (o < len)
-        val = isConst ? uint32_t(cv[base + o]) & 15u : nib(vp[(base + o) * G + g], k);
+        val = isConst ? uint32_t(__ldg(cv + base + o)) & 15u : nib(ldsU32(vpAddr<G>(vp, base + o, g)), k);
       else
         val = nib(OR, k);
       out |= val << (4 * k);
     }
-    vp[res * G + g] = out;
+    stsU32(vpAddr<G>(vp, res, g), out);
   }
 }
 
@@ -239,9 +307,9 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
 // Work item = (op, group, stream), one per lane: the SPW lanes of one (op,
 // group) hold the streams of one word and merge their result nibbles with
 // shuffles, so no lane runs the streams of a word one after another.
-template <int SPW, int G>
-__device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *__restrict__ mp, uint32_t hdr,
-                          uint32_t *__restrict__ vp, uint32_t lane, uint32_t g0, uint32_t gn) {
+template <int SPW, int G, bool SH>
+__device__ void evalVecOp(const KParams &p, const PartDesc &d, const Words<SH> mp, uint32_t hdr, uint32_t vp,
+                          uint32_t lane, uint32_t g0, uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
   const uint32_t total = n * gn * SPW;
   const uint8_t *cv = p.constVec + d.constOff;
@@ -251,7 +319,7 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *_
     const bool act = w < total;
     const uint32_t op = act ? w / (gn * SPW) : 0u;
     const uint32_t g = g0 + (w / SPW) % gn, k = w % SPW;
-    const uint32_t *r = mp + kMPHeaderWords + op * kVecOpWords;
+    const Words<SH> r = mp.at(kMPHeaderWords + op * kVecOpWords);
     const uint32_t w0 = r[0], w1 = r[1], res = r[2];
     const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = act ? (w1 & 0xFFFFu) : 0u, opc = (w1 >> 16) & 0xFFu;
     const uint32_t cf = w1 >> 24;
@@ -259,8 +327,8 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *_
     const bool isVec = opc <= 2;
     unsigned __int128 a = 0, b = 0;
     for (uint32_t i = 0; i < len; ++i) {
-      const uint32_t x = c1 ? (uint32_t(cv[v1 + i]) & 15u) : nib(vp[(v1 + i) * G + g], k);
-      const uint32_t y = c2 ? (uint32_t(cv[v2 + i]) & 15u) : nib(vp[(v2 + i) * G + g], k);
+      const uint32_t x = c1 ? (uint32_t(__ldg(cv + v1 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v1 + i, g)), k);
+      const uint32_t y = c2 ? (uint32_t(__ldg(cv + v2 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v2 + i, g)), k);
       a |= (unsigned __int128)x << (4 * i);
       b |= (unsigned __int128)y << (4 * i);
     }
@@ -289,20 +357,19 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const uint32_t *_
       uint32_t word = i < outLen ? (uint32_t(rv >> (4 * i)) & 15u) << (4 * k) : 0u;
 #pragma unroll
       for (int o = 1; o < SPW; o <<= 1) word |= __shfl_xor_sync(kFull, word, o);
-      if (k == 0 && i < outLen) vp[((res + i) & 0xFFFFu) * G + g] = word;
+      if (k == 0 && i < outLen) stsU32(vpAddr<G>(vp, (res + i) & 0xFFFFu, g), word);
     }
   }
 }
 
 // Memory reads (SimEval.cu:550-575): the loads of the SPW streams of a word
 // are issued together, then merged.
-template <int SPW, int G>
-__device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__restrict__ mp, uint32_t hdr,
-                                            uint32_t *__restrict__ vp, uint32_t lane, uint32_t gb, uint32_t g0,
-                                            uint32_t gn) {
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void evalMemRead(const KParams &p, const Words<SH> mp, uint32_t hdr, uint32_t vp,
+                                            uint32_t lane, uint32_t gb, uint32_t g0, uint32_t gn) {
   const uint32_t n = (hdr >> 2) & 63u;
   if (lane >= n) return;
-  const uint32_t *r = mp + kMPHeaderWords + lane * kMemReadWords;
+  const Words<SH> r = mp.at(kMPHeaderWords + lane * kMemReadWords);
   const uint32_t lo = r[0], hi = r[1], w2 = r[2], res = r[3];
   const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
   const bool multi = (hi >> 31) != 0;
@@ -310,11 +377,11 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
   if (en == 0) return;  // immediate 0: neither reads nor writes (SimEval.cu:559-560)
 #pragma unroll 1
   for (uint32_t g = g0; g < g0 + gn; ++g) {
-    const uint32_t EN = en < 16 ? rep8(en) : vp[en * G + g];
+    const uint32_t EN = en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g));
     uint32_t AD[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) AD[j] = vp[(av + j) * G + g];
-    uint32_t out = vp[res * G + g];  // a disabled read leaves the slot as it is
+    for (int j = 0; j < 8; ++j) AD[j] = ldsU32(vpAddr<G>(vp, av + j, g));
+    uint32_t out = ldsU32(vpAddr<G>(vp, res, g));  // a disabled read leaves the slot as it is
     uint32_t val[SPW];
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
@@ -335,7 +402,7 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
 #pragma unroll
     for (int k = 0; k < SPW; ++k)
       if (val[k] < 16u) out = (out & ~(15u << (4 * k))) | (val[k] << (4 * k));
-    vp[res * G + g] = out;
+    stsU32(vpAddr<G>(vp, res, g), out);
   }
 }
 
@@ -345,29 +412,30 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const uint32_t *__
 // thread is done with the buffer's previous level); every thread waits on the
 // buffer's phase parity before reading it.  Waits are bounded.
 struct Stage {
-  uint32_t *buf[2];
-  uint32_t mb[2];     // shared-memory addresses of the mbarriers
-  uint32_t uses[2];   // completed uses per buffer (phase parity)
+  uint32_t buf0;   // shared address of buffer 0; buffer b at buf0 + b * bytes
+  uint32_t bytes;  // bytes of one buffer
+  uint32_t mb0;    // shared address of mbarrier 0; mbarrier b at mb0 + 8 * b
+  uint32_t phase;  // bit b: phase parity of buffer b's next completion
 };
 
 __device__ __forceinline__ void stageIssue(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words) {
   const uint32_t bytes = words * 4u;
-  const uint32_t dst = uint32_t(__cvta_generic_to_shared(st.buf[b]));
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(st.mb[b]), "r"(bytes) : "memory");
+  const uint32_t dst = st.buf0 + b * st.bytes, mb = st.mb0 + 8u * b;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(st.mb[b])
+               "l"(src), "r"(bytes), "r"(mb)
                : "memory");
 }
 
 __device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t b) {
-  const uint32_t parity = st.uses[b] & 1u;
+  const uint32_t parity = (st.phase >> b) & 1u, mb = st.mb0 + 8u * b;
   uint32_t done = 0;
   unsigned long long t0 = 0;
   for (uint32_t spin = 0; !done; ++spin) {
     asm volatile(
         "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\tselp.u32 %0, 1, 0, P;\n\t}"
         : "=r"(done)
-        : "r"(st.mb[b]), "r"(parity)
+        : "r"(mb), "r"(parity)
         : "memory");
     if (!done) {
       if (spin == 0) t0 = gtimer();
@@ -377,23 +445,57 @@ __device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t 
       }
     }
   }
-  st.uses[b]++;
+  st.phase ^= 1u << b;
   return true;
 }
 
+// The units a warp runs in one exec level (block = the level's words).
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, const Words<SH> blk, uint32_t vp,
+                                         uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
+  const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
+  const Words<SH> units = blk.at(2 + NW);
+  const bool profileMP = (p.flags & kFlagProfileMP) != 0;
+  for (uint32_t u = ub; u < ue; ++u) {
+    // unit word: record offset | first group << 26 | (groups - 1) << 28
+    const uint32_t uw = units[u];
+    const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
+    const uint32_t g0 = (uw >> 26) & 3u, gn = ((uw >> 28) & 3u) + 1u;
+    const uint32_t hdr = mp[0];
+    const long long tm = profileMP ? clock64() : 0;
+    switch (hdr & 3u) {
+      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane); break;  // always every group
+      case kMPVecRead: evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
+      case kMPVecOp: evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
+      default: evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn); break;
+    }
+    __syncwarp();
+    if (profileMP && lane == 0) {
+      const uint32_t id = mp[1];
+      atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
+      atomicAdd(p.mpCount + id, gn);  // groups evaluated
+    }
+  }
+}
+
 // ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
+// vp, tab: shared addresses of the block's value pool and truth table.
 template <int SPW, int G>
-__device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__ vp, const uint8_t *__restrict__ tab,
-                         Stage &st, uint32_t cycle, const uint32_t *retire) {
+__device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t tab, Stage &st, uint32_t cycle,
+                         const uint32_t *retire) {
   const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
   const PartDesc &d = p.parts[pid];
   const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
   const uint2 *ld = p.levelDesc + d.schedOff;
   const uint32_t cap = p.stageWords;
+  // level descriptors (block offset, words) are loaded two levels ahead so
+  // their latency stays off the per-level path
+  const uint2 zero2 = make_uint2(0u, 0u);
+  uint2 cur = d.nLevels > 0 ? ld[0] : zero2;
+  uint2 nxt = d.nLevels > 1 ? ld[1] : zero2;
   // the first exec level streams in while the level-0 reads run
   if (cap && tid == 0 && d.nLevels) {
-    const uint2 l0 = ld[0];
-    if (l0.y <= cap) stageIssue(st, 0, p.sched + l0.x, l0.y);
+    if (cur.y <= cap) stageIssue(st, 0, p.sched + cur.x, cur.y);
   }
 
   // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
@@ -405,51 +507,33 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     for (uint32_t i = tid; i < n; i += nthr) {
       const uint32_t s = __ldg(src + i);
       const uint32_t r = (__ldg(dst + (i >> 1)) >> ((i & 1u) * 16)) & 0xFFFFu;
-      copyInG<G>(vp + r * G, pool + size_t(s) * p.gpad + gb * G);
+      copyInG<G>(vpAddr<G>(vp, r, 0), pool + size_t(s) * p.gpad + gb * G);
     }
   }
   __syncthreads();
 
-  // exec levels: warp w runs the micro-partitions the schedule gave it
+  // exec levels: warp w runs the units the schedule gave it
   for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
-    const uint2 cur = ld[lv];
-    const uint32_t *blk = p.sched + cur.x;
+    const uint2 after = lv + 2 < d.nLevels ? ld[lv + 2] : zero2;
+    bool staged = false;
     if (cap) {
       if (lv > 0) __syncthreads();  // staged buffers are reused every second level
       if (tid == 0 && lv + 1 < d.nLevels) {
-        const uint2 nx = ld[lv + 1];
-        if (nx.y <= cap) stageIssue(st, (lv + 1) & 1u, p.sched + nx.x, nx.y);
+        if (nxt.y <= cap) stageIssue(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y);
       }
       // on a (never expected) wait timeout the level is read from global
       // memory instead: same words, uniform control flow, and the error word
       // ends the launch at the next grid barrier
-      if (cur.y <= cap && stageWait(p, st, lv & 1u)) blk = st.buf[lv & 1u];
-    } else if (lv > 0 && (blk[0] & 1u)) {
+      staged = cur.y <= cap && stageWait(p, st, lv & 1u);
+    } else if (lv > 0 && (__ldg(p.sched + cur.x) & 1u)) {
       __syncthreads();
     }
-    const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
-    const uint32_t *units = blk + 2 + NW;
-    const bool profileMP = (p.flags & kFlagProfileMP) != 0;
-    for (uint32_t u = ub; u < ue; ++u) {
-      // unit word: record offset | first group << 26 | (groups - 1) << 28
-      const uint32_t uw = units[u];
-      const uint32_t *mp = blk + (uw & kUnitOffsetMask);
-      const uint32_t g0 = (uw >> 26) & 3u, gn = ((uw >> 28) & 3u) + 1u;
-      const uint32_t hdr = mp[0];
-      const long long tm = profileMP ? clock64() : 0;
-      switch (hdr & 3u) {
-        case kMPLut: evalLut<SPW, G>(mp, hdr, vp, tab, lane); break;  // always every group
-        case kMPVecRead: evalVecRead<SPW, G>(p, d, mp, hdr, vp, lane, g0, gn); break;
-        case kMPVecOp: evalVecOp<SPW, G>(p, d, mp, hdr, vp, lane, g0, gn); break;
-        default: evalMemRead<SPW, G>(p, mp, hdr, vp, lane, gb, g0, gn); break;
-      }
-      __syncwarp();
-      if (profileMP && lane == 0) {
-        const uint32_t id = mp[1];
-        atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
-        atomicAdd(p.mpCount + id, gn);  // groups evaluated
-      }
-    }
+    if (staged)
+      runLevel<SPW, G, true>(p, d, Words<true>{nullptr, st.buf0 + (lv & 1u) * st.bytes}, vp, tab, lane, warp, NW, gb);
+    else
+      runLevel<SPW, G, false>(p, d, Words<false>{p.sched + cur.x, 0u}, vp, tab, lane, warp, NW, gb);
+    cur = nxt;
+    nxt = after;
   }
   __syncthreads();
 
@@ -478,21 +562,25 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
   if (d.copyKind == 1 && stopExit) {
     for (uint32_t i = tid; i < d.copySlots; i += nthr) {
       uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
+      uint32_t w[G];
+      loadG<G>(vpAddr<G>(vp, d.copySrc + i, 0), w);
 #pragma unroll
-      for (int g = 0; g < G; ++g) dst[g] = (vp[(d.copySrc + i) * G + g] & ~fm[g]) | (__ldcg(dst + g) & fm[g]);
+      for (int g = 0; g < G; ++g) dst[g] = (w[g] & ~fm[g]) | (__ldcg(dst + g) & fm[g]);
     }
   } else if (d.copyKind == 1 && retire) {
     for (uint32_t i = tid; i < d.copySlots; i += nthr) {
       const uint32_t iv = p.initRegs[d.copyDst + i];
       const uint32_t init = SPW == 8 ? rep8(iv) : iv;
       uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
+      uint32_t w[G];
+      loadG<G>(vpAddr<G>(vp, d.copySrc + i, 0), w);
 #pragma unroll
-      for (int g = 0; g < G; ++g) dst[g] = (vp[(d.copySrc + i) * G + g] & ~rm[g]) | (init & rm[g]);
+      for (int g = 0; g < G; ++g) dst[g] = (w[g] & ~rm[g]) | (init & rm[g]);
     }
   } else if (d.copyKind) {
     uint32_t *pool = d.copyKind == 1 ? p.regs : p.exg;
     for (uint32_t i = tid; i < d.copySlots; i += nthr)
-      copyOutG<G>(pool + size_t(d.copyDst + i) * p.gpad + gb * G, vp + (d.copySrc + i) * G);
+      copyOutG<G>(pool + size_t(d.copyDst + i) * p.gpad + gb * G, vpAddr<G>(vp, d.copySrc + i, 0));
   }
   if (d.copyKind != 2) {
     for (uint32_t i = tid; i < d.memWCount * G; i += nthr) {
@@ -502,11 +590,11 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
       const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
       const bool multi = (hi >> 31) != 0;
       const uint32_t av = w2 & 0xFFFFu, dat = w2 >> 16;
-      const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
-      const uint32_t DAT = dat < 16 ? rep8(dat) : vp[dat * G + g];
+      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
+      const uint32_t DAT = dat < 16 ? rep8(dat) : ldsU32(vpAddr<G>(vp, dat, g));
       uint32_t AD[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) AD[j] = vp[(av + j) * G + g];
+      for (int j = 0; j < 8; ++j) AD[j] = ldsU32(vpAddr<G>(vp, av + j, g));
 #pragma unroll
       for (int k = 0; k < SPW; ++k) {
         const uint32_t s = (gb * G + g) * SPW + k;
@@ -527,7 +615,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
       for (uint32_t i = tid; i < d.printCount * G; i += nthr) {
         const uint32_t w = __ldg(p.net + d.printOff + i / G), g = i % G;
         const uint32_t en = w & 0xFFFFu, msg = w >> 16;
-        const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
+        const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
         for (int k = 0; k < SPW; ++k) {
           const uint32_t s = (gb * G + g) * SPW + k;
           if (s < p.nStreams && nib(EN, k) != 0 && msg < p.nPrintMsgs) printf("%s", p.printMsgs[msg]);
@@ -537,7 +625,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t *__restrict__
     for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
       const uint32_t opi = i / G, g = i % G;
       const uint32_t sw = __ldg(p.net + d.stopOff + opi), en = sw & 0xFFFFu;
-      const uint32_t EN = (en < 16 ? rep8(en) : vp[en * G + g]) & ~rm[g];
+      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
       for (int k = 0; k < SPW; ++k) {
         const uint32_t s = (gb * G + g) * SPW + k;
         if (s >= p.nStreams || nib(EN, k) == 0) continue;
@@ -826,24 +914,24 @@ __device__ bool stageTable(const KParams &p, uint8_t *tab) {
 // Shared-memory layout of a block: truth table, two exec-level stage buffers,
 // value pool.  Returns false when staging the table timed out.
 struct BlockSmem {
-  uint8_t *tab;
-  uint32_t *vp;
+  uint32_t tab;  // shared address of the truth table
+  uint32_t vp;   // shared address of the value pool
   Stage st;
 };
 
 __device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsigned long long *stageMbar, BlockSmem &b) {
-  b.tab = smem;
-  b.st.buf[0] = reinterpret_cast<uint32_t *>(smem + kLutTablePadded);
-  b.st.buf[1] = b.st.buf[0] + p.stageWords;
-  b.st.mb[0] = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
-  b.st.mb[1] = uint32_t(__cvta_generic_to_shared(&stageMbar[1]));
-  b.st.uses[0] = b.st.uses[1] = 0;
-  b.vp = b.st.buf[1] + p.stageWords;
+  const uint32_t base = uint32_t(__cvta_generic_to_shared(smem));
+  b.tab = base;
+  b.st.buf0 = base + kLutTablePadded;
+  b.st.bytes = p.stageWords * 4u;
+  b.st.mb0 = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
+  b.st.phase = 0;
+  b.vp = b.st.buf0 + 2u * b.st.bytes;
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb[0]) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb[1]) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0 + 8u) : "memory");
   }
-  const bool staged = stageTable(p, b.tab);
+  const bool staged = stageTable(p, smem);
   __syncthreads();
   return staged;
 }
