@@ -45,7 +45,7 @@ def args_parse():
     p.add_argument("--cycles-per-step", type=int, default=0)
     p.add_argument("--streams", type=int, default=0)
     p.add_argument("--groups", type=int, default=4)
-    p.add_argument("--warps", type=int, default=8)
+    p.add_argument("--warps", type=int, default=0, help="warps per block (0: the design's typical exec-level width)")
     p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
     p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
     p.add_argument("--value-pool", default="compact", choices=["compact", "design"],

@@ -59,7 +59,7 @@ int tgs_destroy(tgs_sim *h);
 /* ---- tuning ----------------------------------------------------------- */
 typedef struct tgs_options {
   uint32_t n_streams;        /* independent design copies (default 1) */
-  uint32_t warps_per_block;  /* 4, 8, 16 or 32 (0 = autotune / default) */
+  uint32_t warps_per_block;  /* 1 to 32; 0 = the most common exec-level width of the design (4..16) */
   uint32_t groups_per_item;  /* 8-stream groups one block evaluates together: 1, 2, 4 */
   uint32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid (0 = max) */
   uint32_t schedule;         /* TGS_SCHED_GREEDY or TGS_SCHED_LEARNED */
@@ -80,7 +80,7 @@ typedef struct tgs_options {
 int tgs_default_options(tgs_options *opt);
 
 /* Autotuner (no counterpart in the reference): times short runs of the loaded
- * design at the handle's stream count over groups_per_item x warps_per_block
+ * design at the handle's stream count over groups_per_item x warps_per_block {4, 6, 8, 12, 16}
  * x blocks_per_sm x mode (x staging), keeps the fastest as the handle's
  * options and resets the state to the initial state.  Micro-partition sizes
  * are fixed by the design file; these are the launch-side knobs. */

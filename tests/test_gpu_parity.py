@@ -64,7 +64,7 @@ def test_batch_parity(designs, name, streams, groups):
     _compare(got, ref)
 
 
-@pytest.mark.parametrize("warps", [4, 16, 32])
+@pytest.mark.parametrize("warps", [0, 3, 4, 6, 12, 16, 32])
 def test_warps_per_block(designs, warps):
     dp, sp, info = designs["wide3op"]
     cycles = np.full(16, 30, np.uint32)

@@ -210,6 +210,27 @@ void fillParams(tgs_sim *h) {
 }
 
 // Launch shape, schedule and per-stream state for the current options.
+// Default warps per block: the most common number of units in an exec level
+// (a LUT micro-partition is one unit, a special one G units), within 4..16,
+// so that a typical level keeps every warp of the block busy.
+uint32_t autoWarps(const DeviceImage &img, uint32_t G) {
+  std::vector<uint64_t> count(33, 0);
+  for (const auto &part : img.mp)
+    for (const auto &lv : part) {
+      uint32_t u = 0;
+      for (const auto &m : lv) u += m.feat.kind == kMPLut ? 1u : G;
+      if (u) count[std::min<uint32_t>(u, 32)]++;
+    }
+  uint32_t best = 8;
+  uint64_t bestN = 0;
+  for (uint32_t u = 1; u <= 32; ++u)
+    if (count[u] > bestN) {
+      bestN = count[u];
+      best = u;
+    }
+  return std::clamp<uint32_t>(best, 4, 16);
+}
+
 void configure(tgs_sim *h) {
   const tgs_options &o = h->opt;
   h->nStreams = std::max<uint32_t>(1, o.n_streams);
@@ -222,8 +243,8 @@ void configure(tgs_sim *h) {
     while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
   }
   h->gpad = (h->groups + G - 1) / G * G;
-  uint32_t NW = o.warps_per_block ? o.warps_per_block : 8;
-  if (NW != 4 && NW != 8 && NW != 16 && NW != 32) throw Error(TGS_ERR_ARG, "warps_per_block must be 4, 8, 16 or 32");
+  uint32_t NW = o.warps_per_block ? o.warps_per_block : autoWarps(h->img, uint32_t(G));
+  if (NW < 1 || NW > 32) throw Error(TGS_ERR_ARG, "warps_per_block must be 1 to 32");
   h->lc.spw = int(h->spw);
   h->lc.G = G;
   h->lc.threads = NW * 32;
@@ -577,7 +598,7 @@ int tgs_default_options(tgs_options *o) {
     if (!o) throw Error(TGS_ERR_ARG, "null options");
     std::memset(o, 0, sizeof(*o));
     o->n_streams = 1;
-    o->warps_per_block = 8;
+    o->warps_per_block = 0;  // the design's typical exec-level width
     o->groups_per_item = 4;
     o->blocks_per_sm = 0;
     o->schedule = TGS_SCHED_GREEDY;
@@ -613,7 +634,7 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
     const tgs_options base = h->opt;
     std::vector<uint32_t> Gs = {1};
     if (h->nStreams > 1) Gs = {1, 2, 4};
-    const uint32_t NWs[] = {4, 8, 16};
+    const uint32_t NWs[] = {4, 6, 8, 12, 16};
     const uint32_t BPS[] = {1, 2, 0};
     std::vector<tgs_tune_trial> all;
     tgs_tune_trial win{};
