@@ -69,7 +69,9 @@ typedef struct tgs_options {
   uint32_t resident_netlist; /* 0: stage each exec level into shared memory when it fits (default); 2: read levels from global memory */
   uint32_t value_pool;       /* 0: renumber value-pool slots by live range (default); 1: the design file's numbering.
                                 Takes effect at the next tgs_init / tgs_init_from_memory */
-  uint32_t reserved[6];
+  uint32_t capture_signals;  /* 1: record every signal of the symbol file each cycle (tgs_read_signal, VCD);
+                                takes effect at the next tgs_init (tgs_enable_vcd also turns it on) */
+  uint32_t reserved[5];
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u
@@ -139,10 +141,25 @@ int tgs_read_register(tgs_sim *h, const char *name, uint64_t *value);
 int tgs_set_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t value);
 int tgs_read_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t *value);
 
-/* ToucanSimulator::readSignal (src/ToucanSim.cu:291-300) is unimplemented in
- * the reference (returns UINT64_MAX).  Here: TGS_ERR_NOT_FOUND for unknown
- * names, otherwise *value = UINT64_MAX as in the reference. */
+/* ToucanSimulator::readSignal (src/ToucanSim.cu:291-300; unimplemented in
+ * the reference, which returns UINT64_MAX): the value of a signal of the
+ * symbol file's signalDebugInfo in the last evaluated cycle.  A signal is a
+ * list of (partition, value-pool slot, width) sections, most significant
+ * first (the order of the reference's VCD writer, unsupport/SimVCD.cpp);
+ * each section's value is the slot's nibble after the partition's exec
+ * levels.  Needs options.capture_signals (else TGS_ERR_STATE); at most 64
+ * bits (TGS_ERR_RANGE).  A section whose slot the partition never writes
+ * has no defined value. */
 int tgs_read_signal(tgs_sim *h, const char *name, uint64_t *value);
+int tgs_read_signal_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t *value);
+/* ToucanSimulator::enableVCDDump (unsupport/SimVCD.cpp:99-241, not built by
+ * the reference): writes a VCD file of every signal of stream 0, one time
+ * step per tgs_eval (#c = the values of cycle c) and one per
+ * tgs_eval_free_running / tgs_eval_until_stop (its last cycle).  Turns signal
+ * capture on, which needs a new device image: allowed before the first
+ * cycle only (TGS_ERR_STATE afterwards) unless capture_signals was set at
+ * init. */
+int tgs_enable_vcd(tgs_sim *h, const char *path);
 
 /* get_real_cycles / setEnablePrint / get_eval_done (src/SimEval.cu:1083-1097) */
 int tgs_get_real_cycles(tgs_sim *h, uint32_t *cycles);
@@ -335,7 +352,8 @@ typedef struct tgs_gen_config {
   uint32_t cone_depth;     /* logic levels per micro-partition (1 = top level only) */
   uint32_t mixed;          /* 1: heterogeneous regions (datapath / control / memory / fan-out) */
   uint32_t with_stop;      /* add a stop op (and print) that fires when a counter saturates */
-  uint32_t reserved[6];
+  uint32_t signals;        /* internal signals listed in the symbol file (signalDebugInfo), 0 = none */
+  uint32_t reserved[5];
 } tgs_gen_config;
 
 typedef struct tgs_gen_info {

@@ -62,6 +62,10 @@ def lib():
         L.orc_state_free.argtypes = [C.c_void_p]
         L.orc_state_eval.restype = C.c_int
         L.orc_state_eval.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
+        L.orc_state_set_probes.restype = C.c_int
+        L.orc_state_set_probes.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
+        L.orc_state_probe_values.restype = C.POINTER(C.c_uint8)
+        L.orc_state_probe_values.argtypes = [C.c_void_p]
         L.orc_state_regs.restype = C.POINTER(C.c_uint8)
         L.orc_state_regs.argtypes = [C.c_void_p]
         L.orc_state_mems.restype = C.POINTER(C.c_uint8)
@@ -158,6 +162,28 @@ class OracleState:
         if lib().orc_state_eval(self._s, cycles, C.byref(stop), err, 512) != 0:
             raise RuntimeError(err.value.decode())
         return bool(stop.value)
+
+    def set_probes(self, parts, slots) -> None:
+        """Record value-pool slot slots[i] of partition parts[i] every cycle."""
+        self._np = len(parts)
+        pa = np.ascontiguousarray(parts, np.uint32)
+        sl = np.ascontiguousarray(slots, np.uint32)
+        if lib().orc_state_set_probes(self._s, pa.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                      sl.ctypes.data_as(C.POINTER(C.c_uint32)), len(pa)) != 0:
+            raise RuntimeError("probe beyond the design")
+
+    def probe_values(self) -> np.ndarray:
+        return np.ctypeslib.as_array(lib().orc_state_probe_values(self._s), (self._np,)).copy()
+
+    def signal(self, sections) -> int:
+        """Value of a signal given as (partition, slot, width) sections, most
+        significant section first, from the probes set for exactly these
+        sections in this order."""
+        v = 0
+        vals = self.probe_values()
+        for (_, _, w), x in zip(sections, vals):
+            v = (v << w) | (int(x) & ((1 << w) - 1))
+        return v
 
     def regs(self) -> np.ndarray:
         return np.ctypeslib.as_array(lib().orc_state_regs(self._s), (self.d.reg_pool,))

@@ -237,6 +237,9 @@ struct EvalCtx {
   const orc_design *d;
   std::vector<uint8_t> vp;  // stale between partitions, like a block's shared memory
   std::string *err;
+  // signal probes: per partition (slot, probe index); values after the exec levels
+  const std::vector<std::vector<std::pair<uint32_t, uint32_t>>> *probes = nullptr;
+  std::vector<uint8_t> *probeValues = nullptr;
 };
 
 // Signed 128-bit sign extension at bit `pos` (SimEval.cu:222-228).
@@ -389,6 +392,8 @@ void evalPartition(EvalCtx &cx, uint32_t pid, StreamState &st, uint32_t cycle, u
   }
   for (auto &lvl : p.levels)
     for (auto &m : lvl) evalMPart(cx, p, m, st);
+  if (cx.probes && pid < cx.probes->size())  // value-pool slots the symbol file names as signals
+    for (auto &pr : (*cx.probes)[pid]) (*cx.probeValues)[pr.second] = vp[pr.first];
 
   if (p.exgWrite.count != 0) {
     // evalLastLevelExgWrite, :732-761.  The op is read from the start of the
@@ -457,6 +462,8 @@ struct orc_state {
   const orc_design *d;
   StreamState st;
   EvalCtx cx;
+  std::vector<std::vector<std::pair<uint32_t, uint32_t>>> probes;
+  std::vector<uint8_t> probeValues;
 };
 
 extern "C" {
@@ -648,6 +655,22 @@ orc_state *orc_state_new(const orc_design *d) {
   return s;
 }
 void orc_state_free(orc_state *s) { delete s; }
+
+// Probes: value-pool slot `slots[i]` of partition `parts[i]` is recorded after
+// that partition's exec levels in every evaluated cycle (the value a signal of
+// the symbol file names); orc_state_probe_values returns the last cycle's.
+int orc_state_set_probes(orc_state *s, const uint32_t *parts, const uint32_t *slots, uint32_t n) {
+  s->probes.assign(s->d->parts.size(), {});
+  for (uint32_t i = 0; i < n; ++i) {
+    if (parts[i] >= s->d->parts.size() || slots[i] >= 65536) return -1;
+    s->probes[parts[i]].push_back({slots[i], i});
+  }
+  s->probeValues.assign(n, 0);
+  s->cx.probes = &s->probes;
+  s->cx.probeValues = &s->probeValues;
+  return 0;
+}
+const uint8_t *orc_state_probe_values(const orc_state *s) { return s->probeValues.data(); }
 uint8_t *orc_state_regs(orc_state *s) { return s->st.regs.data(); }
 uint8_t *orc_state_mems(orc_state *s) { return s->st.mems.data(); }
 

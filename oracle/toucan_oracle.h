@@ -66,6 +66,10 @@ void orc_state_free(orc_state *s);
 int orc_state_eval(orc_state *s, uint32_t cycles, int *stop, char *err, size_t errlen);
 uint8_t *orc_state_regs(orc_state *s);
 uint8_t *orc_state_mems(orc_state *s);
+/* Signal probes: slot slots[i] of partition parts[i], recorded after the
+ * partition's exec levels every cycle; values of the last evaluated cycle. */
+int orc_state_set_probes(orc_state *s, const uint32_t *parts, const uint32_t *slots, uint32_t n);
+const uint8_t *orc_state_probe_values(const orc_state *s);
 uint64_t orc_digest(const uint8_t *pool, size_t n);
 uint64_t orc_mix64(uint64_t x);
 

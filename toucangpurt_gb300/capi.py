@@ -39,7 +39,7 @@ class Options(C.Structure):
         ("n_streams", C.c_uint32), ("warps_per_block", C.c_uint32), ("groups_per_item", C.c_uint32),
         ("blocks_per_sm", C.c_uint32), ("schedule", C.c_uint32), ("mode", C.c_uint32),
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
-        ("value_pool", C.c_uint32), ("reserved", C.c_uint32 * 6),
+        ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("reserved", C.c_uint32 * 5),
     ]
 
 
@@ -74,7 +74,7 @@ class GenConfig(C.Structure):
         ("n_vec_ops", C.c_uint32), ("vec_nibbles", C.c_uint32), ("palette_pct", C.c_uint32),
         ("fanout_alpha", C.c_float), ("max_fanout", C.c_uint32), ("luts_per_part", C.c_uint32),
         ("mpart_width", C.c_uint32), ("cone_depth", C.c_uint32), ("mixed", C.c_uint32), ("with_stop", C.c_uint32),
-        ("reserved", C.c_uint32 * 6),
+        ("signals", C.c_uint32), ("reserved", C.c_uint32 * 5),
     ]
 
 
@@ -174,6 +174,8 @@ SIGNATURES = {
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
     "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_dump_state": [C.c_void_p, C.c_char_p],
+    "tgs_read_signal_stream": [C.c_void_p, C.c_uint32, C.c_char_p, C.POINTER(C.c_uint64)],
+    "tgs_enable_vcd": [C.c_void_p, C.c_char_p],
     "tgs_eval_until_stop": [C.c_void_p, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_uint32)],
     "tgs_load_state": [C.c_void_p, C.c_char_p],
     "tgs_resave_design": [C.c_char_p, C.c_char_p],

@@ -537,6 +537,14 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
   }
   __syncthreads();
 
+  // signal capture: the value-pool slots the symbol file names as signals
+  if (p.probeBuf)
+    for (uint32_t i = tid; i < d.probeCount * G; i += nthr) {
+      const uint32_t pi = i / G, g = i % G;
+      const uint32_t slot = __ldg(p.net + d.probeOff + 2 * pi), idx = __ldg(p.net + d.probeOff + 2 * pi + 1);
+      p.probeBuf[size_t(idx) * p.gpad + gb * G + g] = ldsU32(vpAddr<G>(vp, slot, g));
+    }
+
   // last level (evalLastLevel / evalLastLevelExgWrite, SimEval.cu:625-761)
   // masks of streams retiring this cycle (admission): their registers take
   // the initial values, their memory writes / prints / stops are dropped

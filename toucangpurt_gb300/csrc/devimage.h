@@ -53,7 +53,8 @@ struct PartDesc {
   uint32_t stopCount, stopOff;   // 1 word per op: en
   uint32_t constOff, constLen;   // byte offset / length in the const-vector byte array
   uint32_t region;
-  uint32_t pad[5];
+  uint32_t probeCount, probeOff;  // signal probes: 2 words per probe (slot, probe index)
+  uint32_t pad[3];
 };
 static_assert(sizeof(PartDesc) == 96, "PartDesc size");
 
@@ -140,6 +141,7 @@ struct KParams {
   // device, so one captured chunk serves every call
   uint32_t *graphState;
   uint32_t *nStopped;         // kFlagStopExit: streams stopped so far
+  uint32_t *probeBuf;         // signal capture: [probe][gpad] value-pool words after the exec levels (null = off)
 };
 
 constexpr uint32_t kNoStream = 0xFFFFFFFFu;

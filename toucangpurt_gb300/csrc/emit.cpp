@@ -170,7 +170,7 @@ void accessOf(const CGMicroPartInfo &m, std::vector<uint32_t> &rd, std::vector<u
 
 }  // namespace
 
-void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots) {
+void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, const ProbeList *probes) {
   img = DeviceImage();
   img.parts.resize(d.parts.size());
   img.mp.resize(d.parts.size());
@@ -182,13 +182,17 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots) {
     const SimPartitionInfo &orig = d.parts[pid];
     SimPartitionInfo renamed;
     const SimPartitionInfo *pp = &orig;
+    std::vector<uint32_t> keep, newOf;
+    if (probes && pid < probes->size())
+      for (auto &pr : (*probes)[pid]) keep.push_back(pr.first);
     if (compactSlots) {
-      std::vector<uint32_t> newOf;
-      const uint32_t n = planSlots(orig, newOf);
+      const uint32_t n = planSlots(orig, newOf, keep.empty() ? nullptr : &keep);
       if (n <= 65534) {
         renamed = orig;
         renameSlots(renamed, newOf, n);
         pp = &renamed;
+      } else {
+        newOf.clear();
       }
     }
     const SimPartitionInfo &p = *pp;
@@ -282,6 +286,18 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots) {
       for (size_t i = 0; i < p.ops_last_stop.size(); ++i)
         net.push_back(uint32_t(p.ops_last_stop[i].en) | (uint32_t(orig.ops_last_stop[i].en) << 16));
     }
+    // signal probes: (slot in the image's numbering, probe index)
+    align4(net);
+    pd.probeOff = uint32_t(net.size());
+    if (probes && pid < probes->size())
+      for (auto &pr : (*probes)[pid]) {
+        uint32_t slot = pr.first;
+        if (!newOf.empty()) slot = slot < newOf.size() ? newOf[slot] : kNoSlot;
+        if (slot == kNoSlot || slot >= pd.vpSlots) continue;  // never written here: no value to record
+        net.push_back(slot);
+        net.push_back(pr.second);
+        ++pd.probeCount;
+      }
     pd.constOff = uint32_t(img.constVec.size());
     pd.constLen = uint32_t(p.constVecPool.size());
     img.constVec.insert(img.constVec.end(), p.constVecPool.begin(), p.constVecPool.end());

@@ -60,8 +60,12 @@ struct Schedule {
   uint64_t barriers = 0, levels = 0;
 };
 
-// compactSlots: renumber value-pool slots by live range (slotalloc.h)
-void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots);
+// compactSlots: renumber value-pool slots by live range (slotalloc.h).
+// probes (optional): per partition, (value-pool slot, probe index) pairs
+// whose values the kernel records after the exec levels (signal capture).
+using ProbeList = std::vector<std::vector<std::pair<uint32_t, uint32_t>>>;
+void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots,
+                const ProbeList *probes = nullptr);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
 // G: stream groups per item (special micro-partitions are split by group).
 void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,

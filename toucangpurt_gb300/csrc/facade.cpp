@@ -67,10 +67,13 @@ int ToucanSimulator::init(const int gpu_id, const std::string designBinFilename,
 void ToucanSimulator::enableVCDDump(const std::string vcdFilename) {
   dumpVCD = true;
   vcdFile = vcdFilename;
+  if (sim_ && tgs_enable_vcd(sim_, vcdFilename.c_str()) != TGS_OK) {
+    std::cerr << "enableVCDDump: " << tgs_last_error() << std::endl;
+    dumpVCD = false;
+  }
 }
 
 bool ToucanSimulator::eval() {
-  if (dumpVCD) std::cout << "VCD dump is not supported yet!\n";
   int stop = 0;
   dieOn(tgs_eval(sim_, &stop), "eval");
   cycle_cnt++;
@@ -78,7 +81,6 @@ bool ToucanSimulator::eval() {
 }
 
 bool ToucanSimulator::eval_free_running(uint32_t max_cycles) {
-  if (dumpVCD) std::cout << "VCD dump is not supported yet!\n";
   int stop = 0;
   dieOn(tgs_eval_free_running(sim_, max_cycles, &stop), "eval_free_running");
   cycle_cnt += max_cycles;
@@ -95,9 +97,15 @@ uint64_t ToucanSimulator::readRegister(const std::string &name) {
   return v;
 }
 
-uint64_t ToucanSimulator::readSignal(const std::string &) {
-  std::cerr << "Not implemented! This might not be necessary" << std::endl;
-  return UINT64_MAX;
+// UINT64_MAX with a message when the value is not available (signal capture
+// off, unknown name, wider than 64 bits), as the reference always answers.
+uint64_t ToucanSimulator::readSignal(const std::string &name) {
+  uint64_t v = 0;
+  if (!sim_ || tgs_read_signal(sim_, name.c_str(), &v) != TGS_OK) {
+    std::cerr << "readSignal: " << (sim_ ? tgs_last_error() : "simulator not initialised") << std::endl;
+    return UINT64_MAX;
+  }
+  return v;
 }
 
 void ToucanSimulator::cleanup() {

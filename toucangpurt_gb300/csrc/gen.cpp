@@ -715,6 +715,34 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
   for (uint32_t k = 0; k < P; ++k) d.regionPartitionIds[0].push_back(k);
   for (uint32_t k = 0; k < P; ++k) d.regionPartitionIds[1].push_back(P + k);
 
+  // internal signals: 1-4 sections of value-pool slots written by a LUT
+  // write-back of the partition (drawn from their own generator, so designs
+  // without signals stay as they were)
+  if (c.signals) {
+    Rng srng(c.seed ^ 0x5167A15ull);
+    std::vector<std::vector<uint16_t>> written(d.parts.size());
+    for (size_t pid = 0; pid < d.parts.size(); ++pid) {
+      for (auto &lvl : d.parts[pid].exec_mParts)
+        for (auto &m : lvl)
+          for (auto &w : m.lastLevel) written[pid].push_back(w.result);
+      std::sort(written[pid].begin(), written[pid].end());
+      written[pid].erase(std::unique(written[pid].begin(), written[pid].end()), written[pid].end());
+    }
+    for (uint32_t i = 0; i < c.signals; ++i) {
+      uint32_t pid = srng.below(uint32_t(d.parts.size()));
+      for (uint32_t tries = 0; written[pid].empty() && tries < d.parts.size(); ++tries) pid = (pid + 1) % d.parts.size();
+      if (written[pid].empty()) break;
+      const uint32_t nsec = 1 + srng.below(4);
+      std::vector<std::tuple<uint32_t, uint32_t, uint32_t>> secs;
+      for (uint32_t k = 0; k < nsec; ++k) {
+        const uint16_t slot = written[pid][srng.below(uint32_t(written[pid].size()))];
+        const uint32_t width = (k == 0) ? 1 + srng.below(4) : 4;
+        secs.emplace_back(pid, slot, width);
+      }
+      s.signalDebugInfo["sig_" + std::to_string(i)] = std::move(secs);
+    }
+  }
+
   if (info) {
     std::memset(info, 0, sizeof(*info));
     info->lut_ops = cnt.lut;

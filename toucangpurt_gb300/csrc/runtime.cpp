@@ -12,8 +12,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <fstream>
 #include <iterator>
+#include <map>
 #include <memory>
 #include <queue>
 #include <tuple>
@@ -111,6 +113,20 @@ struct tgs_sim {
   tgs::DBuf<unsigned long long> mpCycles;
   tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, event cursor, end, first cycle, exit
   tgs::DBuf<uint32_t> nStopped;    // stop exit: streams stopped
+  // signal capture (symbol file signalDebugInfo): probe = one (partition,
+  // slot) section; a signal = its sections' probes and widths, most
+  // significant first
+  bool captureSignals = false;
+  tgs::ProbeList probes;
+  uint32_t nProbes = 0;
+  std::map<std::string, std::vector<std::pair<uint32_t, uint32_t>>> signalProbes;  // name -> (probe, width)
+  tgs::DBuf<uint32_t> probeBuf;    // [probe][gpad]
+  // VCD dump (ToucanSimulator::enableVCDDump)
+  std::unique_ptr<std::ofstream> vcd;
+  std::vector<std::string> vcdNames, vcdIds;
+  std::vector<uint32_t> vcdWidths;
+  std::vector<std::string> vcdLast;
+  bool vcdFirst = true;
   // instantiated graph chunks, keyed by the launch parameters they captured
   struct GraphEntry {
     std::vector<uint8_t> key;
@@ -186,6 +202,7 @@ void fillParams(tgs_sim *h) {
   p.barrier = h->barrier.p;
   p.realCycles = h->realCycles.p;
   p.nStopped = h->nStopped.p;
+  p.probeBuf = h->probeBuf.p;
   p.digAcc = h->digAcc.p;
   p.roll = h->roll.p;
   p.cycDig = nullptr;
@@ -321,6 +338,12 @@ void configure(tgs_sim *h) {
   h->seeds.alloc(h->nStreams);
   h->outA.alloc(h->nStreams);
   h->outB.alloc(h->nStreams);
+  if (h->captureSignals && h->nProbes) {
+    h->probeBuf.alloc(size_t(h->nProbes) * h->gpad);
+    TGS_CUDA(cudaMemsetAsync(h->probeBuf.p, 0, size_t(h->nProbes) * h->gpad * 4, h->stream));
+  } else {
+    h->probeBuf.free();
+  }
   fillParams(h);
 }
 
@@ -348,9 +371,40 @@ void setupDevice(tgs_sim *h, int gpu) {
   if (!h->stream) TGS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
 }
 
+// Probes of every signal in the symbol file (option capture_signals).
+void buildProbes(tgs_sim *h) {
+  h->captureSignals = h->opt.capture_signals != 0;
+  h->probes.assign(h->design.parts.size(), {});
+  h->signalProbes.clear();
+  h->nProbes = 0;
+  if (!h->captureSignals) return;
+  std::map<std::pair<uint32_t, uint32_t>, uint32_t> index;
+  std::vector<std::string> names;
+  for (auto &kv : h->symbols.signalDebugInfo) names.push_back(kv.first);
+  std::sort(names.begin(), names.end());
+  for (auto &name : names) {
+    auto &secs = h->symbols.signalDebugInfo.at(name);
+    std::vector<std::pair<uint32_t, uint32_t>> sp;
+    for (auto &t : secs) {
+      const uint32_t part = std::get<0>(t), slot = std::get<1>(t), width = std::get<2>(t);
+      if (part >= h->design.parts.size() || slot >= std::max<uint32_t>(h->design.parts[part].valuePoolSize, 16))
+        throw Error(TGS_ERR_INVALID_DESIGN, "signal " + name + " names a slot beyond its partition's value pool");
+      if (width > 4) throw Error(TGS_ERR_INVALID_DESIGN, "signal " + name + " has a section wider than a nibble");
+      auto it = index.find({part, slot});
+      if (it == index.end()) {
+        it = index.emplace(std::make_pair(part, slot), h->nProbes++).first;
+        h->probes[part].push_back({slot, it->second});
+      }
+      sp.push_back({it->second, width});
+    }
+    h->signalProbes[name] = std::move(sp);
+  }
+}
+
 void upload(tgs_sim *h) {
   cudaStream_t s = h->stream;
-  buildImage(h->design, h->img, h->opt.value_pool == 0);
+  buildProbes(h);
+  buildImage(h->design, h->img, h->opt.value_pool == 0, h->captureSignals ? &h->probes : nullptr);
   h->net.upload(h->img.net, s);
   h->constVec.upload(h->img.constVec, s);
   std::vector<uint8_t> lut(kLutTablePadded, 0);
@@ -536,6 +590,131 @@ void setRegister(tgs_sim *h, uint32_t s, const char *name, uint64_t value) {
 }
 
 // read_reg_from_gpu (SimEval.cu:1058-1069): most significant nibble first.
+// Probe nibbles of one stream (the values of the last evaluated cycle).
+std::vector<uint8_t> probeNibbles(tgs_sim *h, uint32_t s) {
+  if (!h->captureSignals) throw Error(TGS_ERR_STATE, "signal capture is off (set options.capture_signals before tgs_init)");
+  uint32_t g, k;
+  streamPos(h, s, g, k);
+  std::vector<uint32_t> words(std::max<uint32_t>(1, h->nProbes));
+  if (h->nProbes)
+    TGS_CUDA(cudaMemcpy2D(words.data(), 4, h->probeBuf.p + g, size_t(h->gpad) * 4, 4, h->nProbes, cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> out(h->nProbes);
+  for (uint32_t i = 0; i < h->nProbes; ++i) out[i] = uint8_t((words[i] >> (4 * k)) & 15u);
+  return out;
+}
+
+// A signal's value: its sections' low `width` bits, most significant first
+// (the reference's VCD writer order, unsupport/SimVCD.cpp:226-236).
+uint64_t readSignal(tgs_sim *h, uint32_t s, const char *name) {
+  if (!h->symbols.signalDebugInfo.count(name)) throw Error(TGS_ERR_NOT_FOUND, std::string("unknown signal ") + name);
+  const std::vector<uint8_t> nib = probeNibbles(h, s);  // throws when capture is off
+  const auto it = h->signalProbes.find(name);
+  uint32_t bits = 0;
+  uint64_t v = 0;
+  for (auto &pw : it->second) {
+    bits += pw.second;
+    v = (v << pw.second) | (nib[pw.first] & ((1u << pw.second) - 1u));
+  }
+  if (bits > 64) throw Error(TGS_ERR_RANGE, std::string("signal ") + name + " is wider than 64 bits");
+  return v;
+}
+
+// VCD identifier of signal i: base-94 over the printable characters.
+std::string vcdId(uint32_t i) {
+  std::string id;
+  do {
+    id.push_back(char(33 + i % 94));
+    i /= 94;
+  } while (i);
+  return id;
+}
+
+void enableVcd(tgs_sim *h, const char *path) {
+  if (!h->captureSignals) {
+    // signal capture changes the device image: only before the first cycle
+    if (h->cycleCnt != 0) throw Error(TGS_ERR_STATE, "enable the VCD dump before the first cycle");
+    h->opt.capture_signals = 1;
+    upload(h);
+    configure(h);
+    resetState(h);
+  }
+  auto f = std::make_unique<std::ofstream>(path);
+  if (!*f) throw Error(TGS_ERR_IO, std::string("cannot write ") + path);
+  h->vcdNames.clear();
+  h->vcdWidths.clear();
+  for (auto &kv : h->signalProbes) {  // sorted by name
+    uint32_t w = 0;
+    for (auto &pw : kv.second) w += pw.second;
+    h->vcdNames.push_back(kv.first);
+    h->vcdWidths.push_back(std::max<uint32_t>(w, 1));
+  }
+  h->vcdIds.clear();
+  for (uint32_t i = 0; i < h->vcdNames.size(); ++i) h->vcdIds.push_back(vcdId(i));
+  h->vcdLast.assign(h->vcdNames.size(), std::string());
+  h->vcdFirst = true;
+  std::ofstream &o = *f;
+  char date[64];
+  const std::time_t now = std::time(nullptr);
+  std::strftime(date, sizeof date, "%Y-%m-%d %H:%M:%S UTC", std::gmtime(&now));
+  o << "$date\n    " << date << "\n$end\n$version\n    toucan_gb300\n$end\n$timescale\n    1ps\n$end\n";
+  // scopes from the dotted names: a.b.c -> module a, module b, wire c
+  std::vector<std::string> open;
+  for (uint32_t i = 0; i < h->vcdNames.size(); ++i) {
+    std::vector<std::string> parts;
+    std::string cur;
+    for (char ch : h->vcdNames[i]) {
+      if (ch == '.') {
+        parts.push_back(cur);
+        cur.clear();
+      } else {
+        cur.push_back(ch);
+      }
+    }
+    size_t common = 0;
+    while (common < open.size() && common < parts.size() && open[common] == parts[common]) ++common;
+    while (open.size() > common) {
+      o << "$upscope $end\n";
+      open.pop_back();
+    }
+    for (size_t j = common; j < parts.size(); ++j) {
+      o << "$scope module " << parts[j] << " $end\n";
+      open.push_back(parts[j]);
+    }
+    o << "$var wire " << h->vcdWidths[i] << " " << h->vcdIds[i] << " " << cur << " $end\n";
+  }
+  while (!open.empty()) {
+    o << "$upscope $end\n";
+    open.pop_back();
+  }
+  o << "$enddefinitions $end\n$dumpvars\n";
+  h->vcd = std::move(f);
+}
+
+// One VCD time step (stream 0): the signals whose value changed.
+void vcdDump(tgs_sim *h, uint64_t cycle) {
+  if (!h->vcd) return;
+  const std::vector<uint8_t> nib = probeNibbles(h, 0);
+  std::ofstream &o = *h->vcd;
+  o << "#" << cycle << "\n";
+  size_t i = 0;
+  for (auto &kv : h->signalProbes) {
+    std::string bits;
+    for (auto &pw : kv.second)
+      for (int b = int(pw.second) - 1; b >= 0; --b) bits.push_back(char('0' + ((nib[pw.first] >> b) & 1)));
+    if (bits.empty()) bits = "0";
+    if (h->vcdFirst || bits != h->vcdLast[i]) {
+      if (h->vcdWidths[i] == 1)
+        o << bits << h->vcdIds[i] << "\n";
+      else
+        o << "b" << bits << " " << h->vcdIds[i] << "\n";
+      h->vcdLast[i] = bits;
+    }
+    ++i;
+  }
+  h->vcdFirst = false;
+  o.flush();
+}
+
 uint64_t readRegister(tgs_sim *h, uint32_t s, const char *name) {
   const auto &locs = regLocs(h, name);
   uint32_t g, k;
@@ -734,6 +913,7 @@ int tgs_eval(tgs_sim *h, int *stop) {
     runCycles(h, uint32_t(h->cycleCnt), 1, 0);
     TGS_CUDA(cudaStreamSynchronize(h->stream));
     checkDeviceError(h);
+    vcdDump(h, h->cycleCnt);  // time step = the cycle just evaluated
     h->cycleCnt += 1;
     if (stop) *stop = stopFlag(h);
   });
@@ -747,6 +927,7 @@ int tgs_eval_free_running(tgs_sim *h, uint32_t cycles, int *stop) {
     runCycles(h, uint32_t(h->cycleCnt), cycles, kFlagCountCycles | kFlagProfile);
     TGS_CUDA(cudaStreamSynchronize(h->stream));
     checkDeviceError(h);
+    if (cycles) vcdDump(h, h->cycleCnt + cycles - 1);  // signals of the last cycle
     h->cycleCnt += cycles;
     if (stop) *stop = stopFlag(h);
   });
@@ -761,6 +942,7 @@ int tgs_eval_until_stop(tgs_sim *h, uint32_t max_cycles, int *stop, uint32_t *cy
     TGS_CUDA(cudaStreamSynchronize(h->stream));
     checkDeviceError(h);
     TGS_CUDA(cudaMemcpy(&r1, h->realCycles.p, 4, cudaMemcpyDeviceToHost));
+    if (r1 != r0) vcdDump(h, h->cycleCnt + (r1 - r0) - 1);
     h->cycleCnt += r1 - r0;
     if (cycles_run) *cycles_run = r1 - r0;
     if (stop) *stop = stopFlag(h);
@@ -792,8 +974,23 @@ int tgs_read_signal(tgs_sim *h, const char *name, uint64_t *value) {
   return guard([&] {
     requireLoaded(h);
     if (!name || !value) throw Error(TGS_ERR_ARG, "null argument");
-    if (!h->symbols.signalDebugInfo.count(name)) throw Error(TGS_ERR_NOT_FOUND, std::string("unknown signal ") + name);
-    *value = UINT64_MAX;
+    *value = readSignal(h, 0, name);
+  });
+}
+
+int tgs_read_signal_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t *value) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!name || !value) throw Error(TGS_ERR_ARG, "null argument");
+    *value = readSignal(h, stream, name);
+  });
+}
+
+int tgs_enable_vcd(tgs_sim *h, const char *path) {
+  return guard([&] {
+    requireLoaded(h);
+    if (!path) throw Error(TGS_ERR_ARG, "null path");
+    enableVcd(h, path);
   });
 }
 

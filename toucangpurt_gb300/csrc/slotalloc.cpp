@@ -111,9 +111,11 @@ Uses collect(const SimPartitionInfo &p, uint32_t V) {
 
 }  // namespace
 
-uint32_t planSlots(const SimPartitionInfo &p, std::vector<uint32_t> &newOf) {
+uint32_t planSlots(const SimPartitionInfo &p, std::vector<uint32_t> &newOf, const std::vector<uint32_t> *keep) {
   const uint32_t V = std::max<uint32_t>(p.valuePoolSize, 16);
   Uses u = collect(p, V);
+  if (keep)
+    for (uint32_t s : *keep) u.at(s, int32_t(p.exec_mParts.size()) + 1);
   // blocks: maximal runs of slots joined by run constraints
   std::vector<uint32_t> joinNext(V + 1, 0);  // slot s and s + 1 in one block
   for (auto &r : u.runs)

@@ -103,10 +103,18 @@ class Simulator:
     setRegister = set_register
     readRegister = read_register
 
-    def read_signal(self, name: str) -> int:
+    def read_signal(self, name: str, stream: int = 0) -> int:
+        """Value of a symbol-file signal in the last evaluated cycle (needs
+        the capture_signals option)."""
         v = C.c_uint64()
-        check(lib().tgs_read_signal(self._h, name.encode(), C.byref(v)))
+        check(lib().tgs_read_signal_stream(self._h, stream, name.encode(), C.byref(v)))
         return v.value
+
+    readSignal = read_signal
+
+    def enable_vcd(self, path) -> None:
+        """VCD dump of every signal of stream 0 (ToucanSimulator::enableVCDDump)."""
+        check(lib().tgs_enable_vcd(self._h, str(path).encode()))
 
     def real_cycles(self) -> int:
         v = C.c_uint32()
@@ -319,6 +327,39 @@ def mix64(z: np.ndarray) -> np.ndarray:
         z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
         z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
         return z ^ (z >> np.uint64(31))
+
+
+def symbol_signals(symbol_path) -> dict:
+    """signalDebugInfo of a symbol file: name -> [(partition, slot, width)],
+    most significant section first (host-side reader of the reference's
+    symbol format: three maps of u64 count, then per entry a u64-length
+    string, a u64 tuple count and u32 tuples)."""
+    import struct
+
+    b = Path(symbol_path).read_bytes()
+    at = 0
+
+    def u64():
+        nonlocal at
+        v = struct.unpack_from("<Q", b, at)[0]
+        at += 8
+        return v
+
+    def read_map(arity):
+        nonlocal at
+        out = {}
+        for _ in range(u64()):
+            n = u64()
+            key = b[at:at + n].decode()
+            at += n
+            k = u64()
+            vals = struct.unpack_from("<%dI" % (k * arity), b, at)
+            at += 4 * k * arity
+            out[key] = [tuple(vals[i:i + arity]) for i in range(0, len(vals), arity)]
+        return out
+
+    read_map(2)  # registers
+    return read_map(3)
 
 
 def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out: np.ndarray | None = None,
