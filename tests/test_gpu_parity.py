@@ -52,7 +52,7 @@ def _compare(got, ref, cycle_digests=True):
 
 
 @pytest.mark.parametrize("name", list(DESIGNS))
-@pytest.mark.parametrize("streams,groups", [(1, 1), (8, 1), (16, 2), (32, 4), (40, 4)])
+@pytest.mark.parametrize("streams,groups", [(1, 1), (8, 1), (16, 2), (32, 4), (40, 4), (64, 8), (72, 8)])
 def test_batch_parity(designs, name, streams, groups):
     dp, sp, info = designs[name]
     cycles = np.full(streams, 40, np.uint32)

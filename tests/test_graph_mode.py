@@ -29,7 +29,7 @@ def mixed(tmp_path_factory, built):
     return dp, sp, sim.generate(dp, sp, **cfg)
 
 
-@pytest.mark.parametrize("streams,groups,cycles", [(64, 4, 75), (16, 2, 33), (8, 1, 1)])
+@pytest.mark.parametrize("streams,groups,cycles", [(64, 4, 75), (64, 8, 40), (16, 2, 33), (8, 1, 1)])
 def test_graph_batch_matches_oracle(small, streams, groups, cycles):
     """Chunks of 32 cycles replayed; lengths off the chunk boundary skip the tail."""
     dp, sp, info = small

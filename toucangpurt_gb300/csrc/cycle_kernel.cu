@@ -153,7 +153,11 @@ __device__ __forceinline__ uint32_t lookup<8>(uint32_t tab, uint32_t base, uint3
 // ---- value-pool words of G groups ----------------------------------------
 template <int G>
 __device__ __forceinline__ void loadG(uint32_t sa, uint32_t (&v)[G]) {
-  if constexpr (G == 4) {
+  if constexpr (G == 8) {
+    const uint4 q = ldsV4(sa), r = ldsV4(sa + 16u);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    v[4] = r.x; v[5] = r.y; v[6] = r.z; v[7] = r.w;
+  } else if constexpr (G == 4) {
     const uint4 q = ldsV4(sa);
     v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
   } else if constexpr (G == 2) {
@@ -166,7 +170,10 @@ __device__ __forceinline__ void loadG(uint32_t sa, uint32_t (&v)[G]) {
 
 template <int G>
 __device__ __forceinline__ void storeG(uint32_t sa, const uint32_t (&v)[G]) {
-  if constexpr (G == 4) {
+  if constexpr (G == 8) {
+    stsV4(sa, make_uint4(v[0], v[1], v[2], v[3]));
+    stsV4(sa + 16u, make_uint4(v[4], v[5], v[6], v[7]));
+  } else if constexpr (G == 4) {
     stsV4(sa, make_uint4(v[0], v[1], v[2], v[3]));
   } else if constexpr (G == 2) {
     stsV2(sa, make_uint2(v[0], v[1]));
@@ -178,7 +185,10 @@ __device__ __forceinline__ void storeG(uint32_t sa, const uint32_t (&v)[G]) {
 // global (mutable state, L1 bypass) -> value pool
 template <int G>
 __device__ __forceinline__ void copyInG(uint32_t dst, const uint32_t *__restrict__ src) {
-  if constexpr (G == 4) {
+  if constexpr (G == 8) {
+    stsV4(dst, __ldcg(reinterpret_cast<const uint4 *>(src)));
+    stsV4(dst + 16u, __ldcg(reinterpret_cast<const uint4 *>(src) + 1));
+  } else if constexpr (G == 4) {
     stsV4(dst, __ldcg(reinterpret_cast<const uint4 *>(src)));
   } else if constexpr (G == 2) {
     stsV2(dst, __ldcg(reinterpret_cast<const uint2 *>(src)));
@@ -190,7 +200,10 @@ __device__ __forceinline__ void copyInG(uint32_t dst, const uint32_t *__restrict
 // value pool -> global
 template <int G>
 __device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t src) {
-  if constexpr (G == 4) {
+  if constexpr (G == 8) {
+    reinterpret_cast<uint4 *>(dst)[0] = ldsV4(src);
+    reinterpret_cast<uint4 *>(dst)[1] = ldsV4(src + 16u);
+  } else if constexpr (G == 4) {
     *reinterpret_cast<uint4 *>(dst) = ldsV4(src);
   } else if constexpr (G == 2) {
     *reinterpret_cast<uint2 *>(dst) = ldsV2(src);
@@ -200,48 +213,57 @@ __device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t sr
 }
 
 // ---- micro-partitions (evalSingleMicroPart, SimEval.cu:304-580) -----------
-template <int SPW, int G, bool SH>
-__device__ __forceinline__ void evalLut(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane) {
+// One pass of a LUT micro-partition over H stream groups starting at group
+// h0 of the item (value-pool words [slot][G]).
+template <int SPW, int G, int H, bool SH>
+__device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane,
+                                            bool constSlots, uint32_t h0) {
   const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
   const Words<SH> top = mp.at(kMPHeaderWords);
-  uint32_t v[G];
+  uint32_t v[H];
   // top level: operands < 16 are immediates, else value-pool slots
   if (lane < W) {
     const uint2 t = top.pair(2u * lane);
     const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
-    uint32_t A[G], B[G], C[G];
-    if (a < 16) {
-#pragma unroll
-      for (int g = 0; g < G; ++g) A[g] = rep8(a);
+    uint32_t A[H], B[H], C[H];
+    if (constSlots) {
+      loadG<H>(vpAddr<G>(vp, a, h0), A);
+      loadG<H>(vpAddr<G>(vp, b, h0), B);
+      loadG<H>(vpAddr<G>(vp, c, h0), C);
     } else {
-      loadG<G>(vpAddr<G>(vp, a, 0), A);
-    }
-    if (b < 16) {
+      if (a < 16) {
 #pragma unroll
-      for (int g = 0; g < G; ++g) B[g] = rep8(b);
-    } else {
-      loadG<G>(vpAddr<G>(vp, b, 0), B);
-    }
-    if (c < 16) {
+        for (int g = 0; g < H; ++g) A[g] = rep8(a);
+      } else {
+        loadG<H>(vpAddr<G>(vp, a, h0), A);
+      }
+      if (b < 16) {
 #pragma unroll
-      for (int g = 0; g < G; ++g) C[g] = rep8(c);
-    } else {
-      loadG<G>(vpAddr<G>(vp, c, 0), C);
+        for (int g = 0; g < H; ++g) B[g] = rep8(b);
+      } else {
+        loadG<H>(vpAddr<G>(vp, b, h0), B);
+      }
+      if (c < 16) {
+#pragma unroll
+        for (int g = 0; g < H; ++g) C[g] = rep8(c);
+      } else {
+        loadG<H>(vpAddr<G>(vp, c, h0), C);
+      }
     }
 #pragma unroll
-    for (int g = 0; g < G; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
+    for (int g = 0; g < H; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
   } else {
 #pragma unroll
-    for (int g = 0; g < G; ++g) v[g] = 0;
+    for (int g = 0; g < H; ++g) v[g] = 0;
   }
   // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
   const Words<SH> mid = top.at(2u * W);
   for (uint32_t m = 0; m < nMid; ++m) {
     const uint32_t w = lane < W ? mid[m * W + lane] : 0u;
     const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
-    uint32_t nv[G];
+    uint32_t nv[H];
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
+    for (int g = 0; g < H; ++g) {
       const uint32_t As = __shfl_sync(kFull, v[g], int(a6 & 31u));
       const uint32_t Bs = __shfl_sync(kFull, v[g], int(b6 & 31u));
       const uint32_t Cs = __shfl_sync(kFull, v[g], int(c6 & 31u));
@@ -251,19 +273,31 @@ __device__ __forceinline__ void evalLut(const Words<SH> mp, uint32_t hdr, uint32
       nv[g] = lut ? lookup<SPW>(tab, lut, A, B, C) : C;
     }
 #pragma unroll
-    for (int g = 0; g < G; ++g) v[g] = nv[g];
+    for (int g = 0; g < H; ++g) v[g] = nv[g];
   }
   // write-back: shuffleId < 32 immediate, else lane (shuffleId mod 32)
   const Words<SH> wb = mid.at(nMid * W);
   const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;
-  uint32_t out[G];
+  uint32_t out[H];
 #pragma unroll
-  for (int g = 0; g < G; ++g) {
+  for (int g = 0; g < H; ++g) {
     const uint32_t x = __shfl_sync(kFull, v[g], int(src & 31u));
     out[g] = src < 32 ? rep8(src) : x;
   }
-  if (lane < nWB) storeG<G>(vpAddr<G>(vp, res, 0), out);
+  if (lane < nWB) storeG<H>(vpAddr<G>(vp, res, h0), out);
+}
+
+// constSlots: value-pool slots 0..15 hold the immediates 0..15 (renumbered
+// pools never use them), so operands are loaded without a branch.  More than
+// 4 groups run as passes of 4 (the record is read once per pass from shared
+// memory; the unit's bookkeeping is paid once).
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void evalLut(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane,
+                                        bool constSlots) {
+  constexpr int H = G > 4 ? 4 : G;
+#pragma unroll 1
+  for (uint32_t h0 = 0; h0 < uint32_t(G); h0 += H) evalLutPass<SPW, G, H, SH>(mp, hdr, vp, tab, lane, constSlots, h0);
 }
 
 // Special micro-partitions run on the stream groups [g0, g0 + gn) of the
@@ -427,15 +461,19 @@ __device__ __forceinline__ void stageIssue(const Stage &st, uint32_t b, const ui
                : "memory");
 }
 
+// A waiting thread is suspended by the hardware (up to this many ns per try)
+// instead of spinning: no issue slots are spent on the wait.
+constexpr uint32_t kStageSuspendNs = 20000;
+
 __device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t b) {
   const uint32_t parity = (st.phase >> b) & 1u, mb = st.mb0 + 8u * b;
   uint32_t done = 0;
   unsigned long long t0 = 0;
   for (uint32_t spin = 0; !done; ++spin) {
     asm volatile(
-        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\tselp.u32 %0, 1, 0, P;\n\t}"
+        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, P;\n\t}"
         : "=r"(done)
-        : "r"(mb), "r"(parity)
+        : "r"(mb), "r"(parity), "r"(kStageSuspendNs)
         : "memory");
     if (!done) {
       if (spin == 0) t0 = gtimer();
@@ -457,14 +495,14 @@ __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, co
   const Words<SH> units = blk.at(2 + NW);
   const bool profileMP = (p.flags & kFlagProfileMP) != 0;
   for (uint32_t u = ub; u < ue; ++u) {
-    // unit word: record offset | first group << 26 | (groups - 1) << 28
+    // unit word: record offset | first group << 24 | (groups - 1) << 27
     const uint32_t uw = units[u];
     const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
-    const uint32_t g0 = (uw >> 26) & 3u, gn = ((uw >> 28) & 3u) + 1u;
+    const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
     const uint32_t hdr = mp[0];
     const long long tm = profileMP ? clock64() : 0;
     switch (hdr & 3u) {
-      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane); break;  // always every group
+      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0); break;  // always every group
       case kMPVecRead: evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
       case kMPVecOp: evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
       default: evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn); break;
@@ -927,6 +965,7 @@ struct BlockSmem {
   Stage st;
 };
 
+template <int G>
 __device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsigned long long *stageMbar, BlockSmem &b) {
   const uint32_t base = uint32_t(__cvta_generic_to_shared(smem));
   b.tab = base;
@@ -939,6 +978,8 @@ __device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsi
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0 + 8u) : "memory");
   }
+  if (p.constSlots)  // immediates 0..15 in value-pool slots 0..15
+    for (uint32_t i = threadIdx.x; i < 16u * G; i += blockDim.x) stsU32(b.vp + 4u * i, rep8(i / G));
   const bool staged = stageTable(p, smem);
   __syncthreads();
   return staged;
@@ -982,7 +1023,7 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) unsigned long long stageMbar[2];
   BlockSmem b;
-  if (!setupBlock(p, smem, stageMbar, b)) return;
+  if (!setupBlock<G>(p, smem, stageMbar, b)) return;
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
   const uint32_t cEnd = c0 + nCycles;
   uint32_t gen = 0;
@@ -1036,7 +1077,7 @@ __global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k
   const uint32_t t = __ldcg(p.graphState) + k, cEnd = __ldcg(p.graphState + 2);
   if (t >= cEnd || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
   BlockSmem b;
-  if (!setupBlock(p, smem, stageMbar, b)) return;
+  if (!setupBlock<G>(p, smem, stageMbar, b)) return;
   const uint32_t ev = __ldcg(p.graphState + 1);
   const bool event = (p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t;
   regionWork<SPW, G>(p, b, t, r, event, ev, cEnd, __ldcg(p.graphState + 3));
@@ -1155,6 +1196,7 @@ void *cycleKernelPtr() {
 
 void *cycleKernelFor(int spw, int G) {
   if (spw == 1) return cycleKernelPtr<1, 1>();
+  if (G == 8) return cycleKernelPtr<8, 8>();
   if (G == 4) return cycleKernelPtr<8, 4>();
   if (G == 2) return cycleKernelPtr<8, 2>();
   return cycleKernelPtr<8, 1>();
@@ -1169,6 +1211,7 @@ cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint
 
 void *regionKernelFor(int spw, int G) {
   if (spw == 1) return reinterpret_cast<void *>(&regionKernel<1, 1>);
+  if (G == 8) return reinterpret_cast<void *>(&regionKernel<8, 8>);
   if (G == 4) return reinterpret_cast<void *>(&regionKernel<8, 4>);
   if (G == 2) return reinterpret_cast<void *>(&regionKernel<8, 2>);
   return reinterpret_cast<void *>(&regionKernel<8, 1>);

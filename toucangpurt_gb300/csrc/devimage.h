@@ -34,8 +34,8 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 constexpr uint32_t kMPHeaderWords = 4;
 constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;
 // schedule unit word: record offset (words from the level block) | first
-// group << 26 | (groups - 1) << 28
-constexpr uint32_t kUnitOffsetMask = (1u << 26) - 1u;
+// group << 24 | (groups - 1) << 27
+constexpr uint32_t kUnitOffsetMask = (1u << 24) - 1u;
 
 struct PartDesc {
   uint32_t vpSlots;      // value-pool slots (multiple of 4)
@@ -73,6 +73,7 @@ struct KParams {
   const uint32_t *sched;      // exec-level blocks
   const uint2 *levelDesc;     // (block offset, words) per partition level
   uint32_t stageWords;        // capacity of each shared-memory stage buffer (0 = no staging)
+  uint32_t constSlots;        // 1: value-pool slots 0..15 are free (renumbered pools) and hold the immediates
   uint32_t stagePad;
   const PartDesc *parts;
   const uint8_t *constVec;

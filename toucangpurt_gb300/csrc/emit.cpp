@@ -178,6 +178,7 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, con
   for (size_t r = 0; r < d.regionPartitionIds.size(); ++r)
     for (uint32_t id : d.regionPartitionIds[r]) img.partRegion[id] = uint32_t(r);
   auto &net = img.net;
+  img.renumbered = compactSlots;
   for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
     const SimPartitionInfo &orig = d.parts[pid];
     SimPartitionInfo renamed;
@@ -193,6 +194,7 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, con
         pp = &renamed;
       } else {
         newOf.clear();
+        img.renumbered = false;
       }
     }
     const SimPartitionInfo &p = *pp;
@@ -416,7 +418,7 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32
             while (sw.size() % 4) sw.push_back(0);
           }
           if (recordAt[un.i] > kUnitOffsetMask) throw Error(TGS_ERR_RESOURCES, "exec level too large");
-          sw[unitBase + u++] = recordAt[un.i] | (un.g0 << 26) | ((un.gn - 1) << 28);
+          sw[unitBase + u++] = recordAt[un.i] | (un.g0 << 24) | ((un.gn - 1) << 27);
         }
       const uint32_t words = uint32_t(sw.size()) - blk;
       out.levelDesc.push_back(blk);

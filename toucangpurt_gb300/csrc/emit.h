@@ -42,6 +42,7 @@ struct DeviceImage {
   std::vector<std::vector<std::vector<MPartRef>>> mp;  // [part][level][i]
   uint32_t maxVpSlots = 0;
   uint32_t nMParts = 0;
+  bool renumbered = false;  // every partition's slots renumbered (slots 0..15 unused)
 };
 
 struct Schedule {

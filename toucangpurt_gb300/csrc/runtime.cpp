@@ -185,6 +185,7 @@ void fillParams(tgs_sim *h) {
   p.sched = h->schedW.p;
   p.levelDesc = reinterpret_cast<const uint2 *>(h->levelDesc.p);
   p.stageWords = h->stageWords;
+  p.constSlots = h->img.renumbered ? 1u : 0u;
   p.parts = h->parts.p;
   p.constVec = h->constVec.p;
   p.lutTable = h->lutTable.p;
@@ -256,7 +257,7 @@ void configure(tgs_sim *h) {
   int G = 1;
   if (h->spw == 8) {
     G = int(o.groups_per_item ? o.groups_per_item : 4);
-    if (G != 1 && G != 2 && G != 4) throw Error(TGS_ERR_ARG, "groups_per_item must be 1, 2 or 4");
+    if (G != 1 && G != 2 && G != 4 && G != 8) throw Error(TGS_ERR_ARG, "groups_per_item must be 1, 2, 4 or 8");
     while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
   }
   h->gpad = (h->groups + G - 1) / G * G;
@@ -812,7 +813,7 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
     const uint32_t modes = o.modes ? o.modes : 3u;
     const tgs_options base = h->opt;
     std::vector<uint32_t> Gs = {1};
-    if (h->nStreams > 1) Gs = {1, 2, 4};
+    if (h->nStreams > 1) Gs = {1, 2, 4, 8};
     const uint32_t NWs[] = {4, 6, 8, 12, 16};
     const uint32_t BPS[] = {1, 2, 0};
     std::vector<tgs_tune_trial> all;
