@@ -493,22 +493,39 @@ __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, co
                                          uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
   const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
   const Words<SH> units = blk.at(2 + NW);
-  const bool profileMP = (p.flags & kFlagProfileMP) != 0;
+  if (!(p.flags & kFlagProfileMP)) {
+    for (uint32_t u = ub; u < ue; ++u) {
+      // unit word: record offset | first group << 24 | (groups - 1) << 27
+      const uint32_t uw = units[u];
+      const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
+      const uint32_t hdr = mp[0];
+      if ((hdr & 3u) == kMPLut) {
+        evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0);  // always every group
+      } else {
+        const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
+        if ((hdr & 3u) == kMPVecRead) evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
+        else if ((hdr & 3u) == kMPVecOp) evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
+        else evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn);
+      }
+      __syncwarp();
+    }
+    return;
+  }
+  // the same with clock64 around every unit (cost-model samples)
   for (uint32_t u = ub; u < ue; ++u) {
-    // unit word: record offset | first group << 24 | (groups - 1) << 27
     const uint32_t uw = units[u];
     const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
     const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
     const uint32_t hdr = mp[0];
-    const long long tm = profileMP ? clock64() : 0;
+    const long long tm = clock64();
     switch (hdr & 3u) {
-      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0); break;  // always every group
+      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0); break;
       case kMPVecRead: evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
       case kMPVecOp: evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
       default: evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn); break;
     }
     __syncwarp();
-    if (profileMP && lane == 0) {
+    if (lane == 0) {
       const uint32_t id = mp[1];
       atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
       atomicAdd(p.mpCount + id, gn);  // groups evaluated
