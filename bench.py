@@ -44,7 +44,7 @@ def args_parse():
     p.add_argument("--workload", default="largest")
     p.add_argument("--cycles-per-step", type=int, default=0)
     p.add_argument("--streams", type=int, default=0)
-    p.add_argument("--groups", type=int, default=4)
+    p.add_argument("--groups", type=int, default=0, help="8-stream groups per item (0: the library's default)")
     p.add_argument("--warps", type=int, default=0, help="warps per block (0: the design's typical exec-level width)")
     p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
     p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
@@ -291,11 +291,12 @@ def prepare(a, s):
 
 
 def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
-    """Streams of log-uniform length queued onto resident slots (retired and
-    admitted in place inside one persistent launch).  One step = the whole job."""
+    """Streams of log-uniform length queued, longest first, onto resident
+    slots (retired and admitted in place inside one launch or one sequence of
+    graph replays).  One step = the whole job."""
     from toucangpurt_gb300 import sim, workloads
 
-    s = sim.Simulator(n_streams=a.slots or 1024, groups_per_item=a.groups, warps_per_block=a.warps,
+    s = sim.Simulator(n_streams=a.slots or 8, groups_per_item=a.groups, warps_per_block=a.warps,
                       mode=1 if a.mode == "graph" else 0, value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
@@ -323,7 +324,7 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
             "warmup": a.warmup, "ms_per_step": 1000 * dev_s / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
-                                   f"(mean {cyc.mean():.0f}), {st['streams_per_word'] * 0 + (a.slots or min(streams, 1024))} slots",
+                                   f"(mean {cyc.mean():.0f}), {s.options()['n_streams']} slots, longest first",
                        "stream_cycles": int(cyc.sum()), "blocks": st["blocks"], "threads_per_block": st["threads"],
                        "groups_per_item": st["groups_per_item"], **notes},
             "lut_evals_per_s": total / dev_s * st["lut_ops"],

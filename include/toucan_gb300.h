@@ -60,7 +60,8 @@ int tgs_destroy(tgs_sim *h);
 typedef struct tgs_options {
   uint32_t n_streams;        /* independent design copies (default 1) */
   uint32_t warps_per_block;  /* 1 to 32; 0 = the most common exec-level width of the design (4..16) */
-  uint32_t groups_per_item;  /* 8-stream groups one block evaluates together: 1, 2, 4 or 8 */
+  uint32_t groups_per_item;  /* 8-stream groups one block evaluates together: 1, 2, 4 or 8; 0 = 4, halved
+                                while a region would have fewer than two items per SM */
   uint32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid (0 = max) */
   uint32_t schedule;         /* TGS_SCHED_GREEDY or TGS_SCHED_LEARNED */
   uint32_t mode;             /* TGS_MODE_PERSISTENT or TGS_MODE_GRAPH */
@@ -243,7 +244,8 @@ typedef struct tgs_batch {
   const uint32_t *cycles;   /* cycles per stream */
   const tgs_stimulus *stim; /* NULL = free running */
   uint32_t flags;
-  uint32_t slots;           /* resident streams (multiple of 8, 0 = options.n_streams) */
+  uint32_t slots;           /* resident streams (rounded up to a multiple of 8); 0 = total cycles / longest
+                               stream (clamped to 8..4096): queued streams are admitted longest first */
 } tgs_batch;
 
 typedef struct tgs_batch_result {
@@ -262,9 +264,9 @@ typedef struct tgs_batch_result {
 
 /* Runs every stream of the job from the initial state.  With equal lengths
  * and all streams resident, one launch runs them side by side.  Otherwise
- * the streams are queued onto `slots` resident slots (default min(n, 1024)):
+ * the streams are queued, longest first, onto `slots` resident slots:
  * a slot whose stream finished is retired and refilled in place by the next
- * queued stream inside the same persistent launch (final digests, rolling
+ * queued stream inside the same launch (final digests, rolling
  * digests, per-cycle digests and stop cycles are reported per job stream;
  * final_regs / final_mems are not available in that form). */
 int tgs_batch_run(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res);

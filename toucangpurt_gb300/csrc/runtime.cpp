@@ -17,6 +17,7 @@
 #include <iterator>
 #include <map>
 #include <memory>
+#include <numeric>
 #include <queue>
 #include <tuple>
 #include <string>
@@ -256,8 +257,18 @@ void configure(tgs_sim *h) {
   h->groups = (h->nStreams + h->spw - 1) / h->spw;
   int G = 1;
   if (h->spw == 8) {
-    G = int(o.groups_per_item ? o.groups_per_item : 4);
-    if (G != 1 && G != 2 && G != 4 && G != 8) throw Error(TGS_ERR_ARG, "groups_per_item must be 1, 2, 4 or 8");
+    if (o.groups_per_item) {
+      G = int(o.groups_per_item);
+      if (G != 1 && G != 2 && G != 4 && G != 8) throw Error(TGS_ERR_ARG, "groups_per_item must be 1, 2, 4 or 8");
+    } else {
+      // default: 4 groups per item (independent work per warp) while a
+      // region still has two items per SM; fewer for few, narrow partitions
+      size_t parts = 1;
+      for (auto &r : h->design.regionPartitionIds) parts = std::max(parts, r.size());
+      const size_t want = 2 * size_t(std::max(1, h->props.multiProcessorCount));
+      G = 4;
+      while (G > 1 && parts * ((h->groups + G - 1) / G) < want) G >>= 1;
+    }
     while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
   }
   h->gpad = (h->groups + G - 1) / G * G;
@@ -779,7 +790,7 @@ int tgs_default_options(tgs_options *o) {
     std::memset(o, 0, sizeof(*o));
     o->n_streams = 1;
     o->warps_per_block = 0;  // the design's typical exec-level width
-    o->groups_per_item = 4;
+    o->groups_per_item = 0;  // 4, or fewer when a region would have too few items
     o->blocks_per_sm = 0;
     o->schedule = TGS_SCHED_GREEDY;
     o->mode = TGS_MODE_PERSISTENT;
@@ -1378,7 +1389,16 @@ float runTimed(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
 // (global cycle, slot, next stream); the kernel follows the event list.
 void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uint32_t flags) {
   const uint32_t n = job->n_streams;
-  uint32_t S = job->slots ? job->slots : std::min<uint32_t>(n, 1024);
+  // default slot count: enough that the queue's work fills the longest
+  // stream's run (longest first keeps that stream from finishing late);
+  // more slots only make every cycle wider
+  uint64_t total = 0, longest = 1;
+  for (uint32_t q = 0; q < n; ++q) {
+    total += job->cycles[q];
+    longest = std::max<uint64_t>(longest, job->cycles[q]);
+  }
+  uint32_t S = job->slots ? job->slots
+                          : uint32_t(std::clamp<uint64_t>((total + longest - 1) / longest, 8, 4096));
   S = std::min(S, n);
   if (S > 1) S = (S + 7) / 8 * 8;
   if (res && (res->final_regs || res->final_mems))
@@ -1394,14 +1414,20 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
     h->opt.n_streams = S;
     configure(h);
   }
-  // queue simulation: min-heap of (retire cycle, slot)
+  // queue simulation: min-heap of (retire cycle, slot).  Streams are admitted
+  // longest first (LPT): every stream's results are independent of when it
+  // runs, and the longest ones no longer start late and run on alone.
+  std::vector<uint32_t> order(n);
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return job->cycles[a] > job->cycles[b]; });
   std::vector<uint32_t> slotStream(S, kNoStream), slotStart(S, 0), slotRetire(S, 0xFFFFFFFFu);
   using E = std::pair<uint64_t, uint32_t>;
   std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
   for (uint32_t s = 0; s < S && s < n; ++s) {
-    slotStream[s] = s;
-    slotRetire[s] = job->cycles[s];
-    pq.push({job->cycles[s], s});
+    const uint32_t q = order[s];
+    slotStream[s] = q;
+    slotRetire[s] = job->cycles[q];
+    pq.push({job->cycles[q], s});
   }
   std::vector<std::tuple<uint64_t, uint32_t, uint32_t>> evs;  // (cycle, slot, next)
   uint32_t nextQ = std::min(S, n);
@@ -1410,7 +1436,7 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
     pq.pop();
     uint32_t qn = kNoStream;
     if (nextQ < n) {
-      qn = nextQ++;
+      qn = order[nextQ++];
       pq.push({t + 1 + job->cycles[qn], s});
     }
     evs.emplace_back(t, s, qn);
@@ -1489,8 +1515,6 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
   const float ms = runTimed(h, 0, uint32_t(last) + 1, flags | kFlagSlots);
   h->cycleCnt = last + 1;
   if (!res) return;
-  uint64_t total = 0;
-  for (uint32_t q = 0; q < n; ++q) total += job->cycles[q];
   res->device_ms = ms;
   res->stream_cycles = total;
   res->launches = h->lastLaunches;
