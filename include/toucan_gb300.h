@@ -235,17 +235,19 @@ typedef struct tgs_stimulus {
 #define TGS_BATCH_ROLLING 2u       /* fill rolling_digest[] */
 #define TGS_BATCH_FINAL_STATE 4u   /* fill final_regs[] / final_mems[] */
 #define TGS_BATCH_CONTINUE 8u      /* continue every stream from the previous call's state and cycle */
-#define TGS_BATCH_STOP_EXIT 16u    /* a stream that executes a stop op freezes after that cycle (registers,
-                                      memories, digests); the launch ends once every stream stopped.
-                                      Streams must all be resident (no queueing). */
+#define TGS_BATCH_STOP_EXIT 16u    /* a stream that executes a stop op ends after that cycle (registers,
+                                      memories, digests freeze); resident streams: the launch ends once every
+                                      stream stopped; queued streams: the stopped stream retires and its slot
+                                      takes the next queued stream. */
 
 typedef struct tgs_batch {
   uint32_t n_streams;       /* streams in the job (may exceed resident slots) */
   const uint32_t *cycles;   /* cycles per stream */
   const tgs_stimulus *stim; /* NULL = free running */
   uint32_t flags;
-  uint32_t slots;           /* resident streams (rounded up to a multiple of 8); 0 = total cycles / longest
-                               stream (clamped to 8..4096): queued streams are admitted longest first */
+  uint32_t slots;           /* resident streams (rounded up to a multiple of 8, at most 4096 when streams
+                               queue); 0 = total cycles / longest stream (clamped to 8..4096): queued
+                               streams are admitted longest first */
 } tgs_batch;
 
 typedef struct tgs_batch_result {
@@ -258,7 +260,7 @@ typedef struct tgs_batch_result {
   uint8_t *final_regs;        /* [n_streams * regPoolSize] */
   uint8_t *final_mems;        /* [n_streams * memPoolSize] */
   double device_ms;           /* time of the device work */
-  uint64_t stream_cycles;     /* total simulated stream-cycles */
+  uint64_t stream_cycles;     /* total simulated stream-cycles (stop exit: through each stop cycle) */
   uint32_t launches;          /* kernel launches issued */
 } tgs_batch_result;
 
@@ -353,7 +355,8 @@ typedef struct tgs_gen_config {
   uint32_t mpart_width;    /* lanes per micro-partition level (<= 32) */
   uint32_t cone_depth;     /* logic levels per micro-partition (1 = top level only) */
   uint32_t mixed;          /* 1: heterogeneous regions (datapath / control / memory / fan-out) */
-  uint32_t with_stop;      /* add a stop op (and print) that fires when a counter saturates */
+  uint32_t with_stop;      /* add a stop op (and print): 1 enabled by a design value (fires early),
+                              2 enabled when a design value equals a constant (about 1 cycle in 16) */
   uint32_t signals;        /* internal signals listed in the symbol file (signalDebugInfo), 0 = none */
   uint32_t reserved[5];
 } tgs_gen_config;

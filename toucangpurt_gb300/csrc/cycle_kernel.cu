@@ -607,9 +607,10 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
 #pragma unroll
   for (int g = 0; g < G; ++g) rm[g] = retire ? __ldcg(retire + gb * G + g) : 0u;
   // stop exit: streams stopped in an earlier cycle keep their state; their
-  // register words are rewritten with the values they hold
+  // register words are rewritten with the values they hold (a stopped stream
+  // that retires now takes the initial values instead)
   const bool stopExit = (p.flags & kFlagStopExit) != 0;
-  uint32_t fm[G];
+  uint32_t fm[G], xm[G];
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     fm[g] = 0;
@@ -619,26 +620,26 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
         const uint32_t s = (gb * G + g) * SPW + k;
         if (s < p.nStreams && __ldcg(p.stopCycle + s) < cycle) fm[g] |= 15u << (4 * k);
       }
-      rm[g] |= fm[g];
+      fm[g] &= ~rm[g];
     }
+    xm[g] = rm[g] | fm[g];  // streams whose writes are dropped this cycle
   }
-  if (d.copyKind == 1 && stopExit) {
+  if (d.copyKind == 1 && (stopExit || retire)) {
     for (uint32_t i = tid; i < d.copySlots; i += nthr) {
+      uint32_t init = 0;
+      if (retire) {
+        const uint32_t iv = p.initRegs[d.copyDst + i];
+        init = SPW == 8 ? rep8(iv) : iv;
+      }
       uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
       uint32_t w[G];
       loadG<G>(vpAddr<G>(vp, d.copySrc + i, 0), w);
 #pragma unroll
-      for (int g = 0; g < G; ++g) dst[g] = (w[g] & ~fm[g]) | (__ldcg(dst + g) & fm[g]);
-    }
-  } else if (d.copyKind == 1 && retire) {
-    for (uint32_t i = tid; i < d.copySlots; i += nthr) {
-      const uint32_t iv = p.initRegs[d.copyDst + i];
-      const uint32_t init = SPW == 8 ? rep8(iv) : iv;
-      uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
-      uint32_t w[G];
-      loadG<G>(vpAddr<G>(vp, d.copySrc + i, 0), w);
-#pragma unroll
-      for (int g = 0; g < G; ++g) dst[g] = (w[g] & ~rm[g]) | (init & rm[g]);
+      for (int g = 0; g < G; ++g) {
+        uint32_t v = (w[g] & ~xm[g]) | (init & rm[g]);
+        if (stopExit) v |= __ldcg(dst + g) & fm[g];
+        dst[g] = v;
+      }
     }
   } else if (d.copyKind) {
     uint32_t *pool = d.copyKind == 1 ? p.regs : p.exg;
@@ -653,7 +654,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
       const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
       const bool multi = (hi >> 31) != 0;
       const uint32_t av = w2 & 0xFFFFu, dat = w2 >> 16;
-      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
+      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
       const uint32_t DAT = dat < 16 ? rep8(dat) : ldsU32(vpAddr<G>(vp, dat, g));
       uint32_t AD[8];
 #pragma unroll
@@ -678,7 +679,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
       for (uint32_t i = tid; i < d.printCount * G; i += nthr) {
         const uint32_t w = __ldg(p.net + d.printOff + i / G), g = i % G;
         const uint32_t en = w & 0xFFFFu, msg = w >> 16;
-        const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
+        const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
         for (int k = 0; k < SPW; ++k) {
           const uint32_t s = (gb * G + g) * SPW + k;
           if (s < p.nStreams && nib(EN, k) != 0 && msg < p.nPrintMsgs) printf("%s", p.printMsgs[msg]);
@@ -688,13 +689,16 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
     for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
       const uint32_t opi = i / G, g = i % G;
       const uint32_t sw = __ldg(p.net + d.stopOff + opi), en = sw & 0xFFFFu;
-      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~rm[g];
+      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
       for (int k = 0; k < SPW; ++k) {
         const uint32_t s = (gb * G + g) * SPW + k;
         if (s >= p.nStreams || nib(EN, k) == 0) continue;
         if (atomicExch(p.stop + s, 1u) == 0u) {
           p.stopCycle[s] = cycle;
-          if (stopExit) atomicAdd(p.nStopped, 1u);
+          if (stopExit) {
+            atomicAdd(p.nStopped, 1u);
+            if (p.flags & kFlagSlots) p.eventHint[2u + (cycle & 1u)] = cycle + 1u;  // a retirement next cycle
+          }
           if (p.printDiag) {
             printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, sw >> 16, nib(EN, k));
             for (uint32_t q = 0; q < d.printCount; ++q) {
@@ -763,14 +767,26 @@ __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, u
   }
 }
 
+// A slot retires in cycle t when its stream's last cycle was t - 1: the
+// stream's length was reached, or (stop exit) it executed a stop op in t - 1.
+__device__ __forceinline__ bool retiringAt(const KParams &p, uint32_t s, uint32_t t) {
+  if (__ldcg(p.slotStream + s) == kNoStream) return false;
+  if (__ldcg(p.slotRetire + s) == t) return true;
+  if (!(p.flags & kFlagStopExit)) return false;
+  const uint32_t sc = __ldcg(p.stopCycle + s);
+  return sc != 0xFFFFFFFFu && sc + 1u == t;
+}
+
 // Streams whose register digest this cycle contributes: every active stream
 // with per-cycle digests, else (admission) only the streams retiring now.
 __device__ __forceinline__ bool digestStream(const KParams &p, uint32_t s, uint32_t cycle) {
   if (s >= p.nStreams) return false;
-  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;
-  if (!(p.flags & kFlagSlots)) return true;
-  if (__ldcg(p.slotStream + s) == kNoStream) return false;
-  return (p.flags & kFlagDigest) || __ldcg(p.slotRetire + s) == cycle;
+  if (p.flags & kFlagSlots) {
+    if (__ldcg(p.slotStream + s) == kNoStream) return false;
+    if (retiringAt(p, s, cycle)) return true;  // the retiring stream's final register digest
+  }
+  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;  // frozen
+  return !(p.flags & kFlagSlots) || (p.flags & kFlagDigest);
 }
 
 // Per-cycle register digest: sum over i of mix64(i << 8 | nibble), per stream.
@@ -813,7 +829,7 @@ __device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint
     if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) continue;
     if (p.flags & kFlagSlots) {
       q = __ldcg(p.slotStream + s);
-      if (q == kNoStream || __ldcg(p.slotRetire + s) == cycle) continue;  // retiring: kept for the admin phase
+      if (q == kNoStream || retiringAt(p, s, cycle)) continue;  // retiring: kept for the admin phase
       lc = cycle - __ldcg(p.slotStart + s);
     }
     const unsigned long long dg = __ldcg(p.digAcc + s);
@@ -824,20 +840,100 @@ __device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint
 }
 
 // ---- admission events --------------------------------------------------------
-// Region 0 of a retire cycle: mark the retiring slots and digest their memories.
+// Retirements are found on the device: a stream may end at its length or, with
+// stop exit, at its stop op, so no list is fixed in advance.  Queued streams
+// are admitted in the order of queueOrder (longest first).
+//
+// A cycle is scanned only when a slot may retire in it.  eventHint words:
+// [t & 1] a lower bound of the next length retirement as of cycle t (a scan
+// in cycle t writes the bound for t + 1, admissions lower it; the graph form
+// carries it from cycle to cycle, the persistent form keeps it in a register
+// between scans); [2 + (c & 1)] = c + 1 when a stream stopped in cycle c.
+// The words read in cycle t are written only in earlier cycles, so every block
+// takes the same decision.
+__device__ __forceinline__ bool mayRetire(const KParams &p, uint32_t t, uint32_t hint) {
+  return t >= hint || ((p.flags & kFlagStopExit) && __ldcg(p.eventHint + 2u + ((t - 1u) & 1u)) == t);
+}
+
+// Every block builds the same bitmask of the slots retiring in cycle t (the
+// state it reads was last written before this cycle's first region) and gets
+// their number; block 0 writes the next length-retirement bound.
+__device__ uint32_t scanRetiring(const KParams &p, uint32_t t, uint32_t *bits) {
+  __shared__ uint32_t count, nextMin;
+  const bool stopExit = (p.flags & kFlagStopExit) != 0;
+  if (threadIdx.x == 0) {
+    count = 0;
+    nextMin = 0xFFFFFFFFu;
+  }
+  __syncthreads();
+  const uint32_t nw = (p.nStreams + 31u) / 32u, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t NW = blockDim.x >> 5;
+  uint32_t c = 0, mn = 0xFFFFFFFFu;
+  for (uint32_t w = warp; w < nw; w += NW) {
+    const uint32_t s = w * 32u + lane;
+    bool ret = false;
+    if (s < p.nStreams) {
+      const uint32_t q = __ldcg(p.slotStream + s), re = __ldcg(p.slotRetire + s), sc = __ldcg(p.stopCycle + s);
+      if (q != kNoStream) {
+        ret = re == t || (stopExit && sc != 0xFFFFFFFFu && sc + 1u == t);
+        if (!ret) mn = min(mn, re);
+      }
+    }
+    const uint32_t m = __ballot_sync(kFull, ret);
+    if (lane == 0) {
+      bits[w] = m;
+      c += __popc(m);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, o));
+  if (lane == 0) {
+    if (c) atomicAdd(&count, c);
+    if (blockIdx.x == 0) atomicMin(&nextMin, mn);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.eventHint[(t + 1u) & 1u] = nextMin;
+  return count;
+}
+
+// The j-th set bit of the bitmask.
+__device__ __forceinline__ uint32_t nthRetiring(const uint32_t *bits, uint32_t nw, uint32_t j) {
+  for (uint32_t w = 0; w < nw; ++w) {
+    uint32_t m = bits[w];
+    const uint32_t c = __popc(m);
+    if (j < c) {
+      for (; j; --j) m &= m - 1u;
+      return w * 32u + uint32_t(__ffs(int(m))) - 1u;
+    }
+    j -= c;
+  }
+  return 0xFFFFFFFFu;
+}
+
+// Region 0 of cycle t: list the retiring slots (block 0: the list, the count,
+// the queue position and the retire masks) and digest their memories.
 template <int SPW>
-__device__ void eventRegion0(const KParams &p, uint32_t ev) {
-  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
-  if (blockIdx.x == 0)
-    for (uint32_t j = eb + threadIdx.x; j < ee; j += blockDim.x) {
-      const uint32_t s = __ldg(p.eventSlot + j);
+__device__ void eventRegion0(const KParams &p, const uint32_t *bits, uint32_t cnt) {
+  const uint32_t nw = (p.nStreams + 31u) / 32u;
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) {
+      *p.retCount = cnt;
+      if (cnt) {
+        uint32_t j = 0;
+        for (uint32_t w = 0; w < nw; ++w)
+          for (uint32_t m = bits[w]; m; m &= m - 1u) p.retList[j++] = w * 32u + uint32_t(__ffs(int(m))) - 1u;
+        *p.queueSnap = __ldcg(p.queueHead);
+      }
+    }
+    for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+      const uint32_t s = nthRetiring(bits, nw, j);
       atomicOr(p.retireMask + s / SPW, 15u << (4 * (s % SPW)));
     }
+  }
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
   const uint32_t chunk = 8192, chunks = (p.memPoolSize + chunk - 1) / chunk;
-  const uint32_t units = (ee - eb) * chunks;
+  const uint32_t units = cnt * chunks;
   for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
-    const uint32_t s = __ldg(p.eventSlot + eb + u / chunks), ch = u % chunks;
+    const uint32_t s = nthRetiring(bits, nw, u / chunks), ch = u % chunks;
     const uint8_t *m = p.mems + s * p.memStride;
     unsigned long long a = 0;
     const uint32_t end = min(p.memPoolSize, (ch + 1) * chunk);
@@ -849,30 +945,33 @@ __device__ void eventRegion0(const KParams &p, uint32_t ev) {
 
 // Region 1 of a retire cycle: reset the retiring slots' memories (their
 // memory writes are dropped this cycle).
-__device__ void eventRegion1(const KParams &p, uint32_t ev, uint32_t gtid, uint32_t gthreads) {
-  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
+__device__ void eventRegion1(const KParams &p, uint32_t gtid, uint32_t gthreads) {
+  const uint32_t cnt = __ldcg(p.retCount);
   const uint32_t vecs = uint32_t((p.memPoolSize + 15ull) / 16);
-  const size_t total = size_t(ee - eb) * vecs;
+  const size_t total = size_t(cnt) * vecs;
   for (size_t i = gtid; i < total; i += gthreads) {
-    const uint32_t s = __ldg(p.eventSlot + eb + uint32_t(i / vecs));
+    const uint32_t s = __ldcg(p.retList + uint32_t(i / vecs));
     const size_t v = i % vecs;
     reinterpret_cast<uint4 *>(p.mems + s * p.memStride)[v] = __ldg(reinterpret_cast<const uint4 *>(p.initMems) + v);
   }
 }
 
 // After the region-1 barrier: publish the retired streams' results and admit
-// the next queued stream into each slot (with its cycle-0 inputs).
+// the next queued streams, in queue order, into the listed slots (with their
+// cycle-0 inputs).
 template <int SPW>
-__device__ void eventAdmit(const KParams &p, uint32_t ev, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
-  const uint32_t eb = __ldg(p.eventBegin + ev), ee = __ldg(p.eventBegin + ev + 1);
-  for (uint32_t j = eb + gtid; j < ee; j += gthreads) {
-    const uint32_t s = __ldg(p.eventSlot + j), qn = __ldg(p.eventNext + j);
+__device__ void eventAdmit(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
+  const uint32_t cnt = __ldcg(p.retCount), head = __ldcg(p.queueSnap);
+  for (uint32_t j = gtid; j < cnt; j += gthreads) {
+    const uint32_t s = __ldcg(p.retList + j);
+    const uint32_t qn = head + j < p.nJobs ? __ldg(p.queueOrder + head + j) : kNoStream;
     const uint32_t q = __ldcg(p.slotStream + s), start = __ldcg(p.slotStart + s);
     p.outReg[q] = __ldcg(p.digAcc + s);
     p.outMem[q] = __ldcg(p.memAcc + s);
     p.outRoll[q] = __ldcg(p.roll + s);
     const uint32_t sc = __ldcg(p.stopCycle + s);
     p.outStop[q] = sc == 0xFFFFFFFFu ? sc : sc - start;
+    atomicAdd(p.nDone, 1u);
     p.digAcc[s] = 0;
     p.memAcc[s] = 0;
     p.roll[s] = 0;
@@ -887,6 +986,7 @@ __device__ void eventAdmit(const KParams &p, uint32_t ev, uint32_t cycle, uint32
     p.slotStream[s] = qn;
     p.slotStart[s] = cycle + 1;
     p.slotRetire[s] = cycle + 1 + __ldg(p.jobLen + qn);
+    atomicMin(p.eventHint + ((cycle + 1u) & 1u), cycle + 1 + __ldg(p.jobLen + qn));
     // primary inputs restart from the initial register values
     for (uint32_t inp = 0; inp < p.nStim; ++inp) {
       const uint32_t reg = __ldg(p.stimReg + inp);
@@ -904,6 +1004,7 @@ __device__ void eventAdmit(const KParams &p, uint32_t ev, uint32_t cycle, uint32
       atomicOr(wp, v << (4 * k));
     }
   }
+  if (gtid == 0) *p.queueHead = min(head + cnt, p.nJobs);
 }
 
 // ---- grid barrier (bounded) --------------------------------------------------
@@ -1006,8 +1107,8 @@ __device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsi
 // work (digests and retiring-stream capture in region 0; memory reset of
 // retiring streams, next cycle's inputs and digest folding in region 1).
 template <int SPW, int G>
-__device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t r, bool event, uint32_t ev,
-                           uint32_t cEnd, uint32_t c0) {
+__device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t r, bool event, const uint32_t *retBits,
+                           uint32_t retCnt, uint32_t cEnd, uint32_t c0) {
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
   const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
   const uint32_t i0 = __ldg(ib + blockIdx.x), i1 = __ldg(ib + blockIdx.x + 1);
@@ -1024,9 +1125,9 @@ __device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t 
   }
   if (r == 0) {
     if ((p.flags & kFlagDigest) || event) digestSlice<SPW>(p, t);
-    if (event) eventRegion0<SPW>(p, ev);
+    if (p.flags & kFlagSlots) eventRegion0<SPW>(p, retBits, retCnt);  // the cycle's list, also when empty
   } else {
-    if (event) eventRegion1(p, ev, gtid, gthreads);
+    if (event) eventRegion1(p, gtid, gthreads);
     // (stop exit: applied after the region barrier, when every stop of the cycle is known)
     if ((p.flags & kFlagStimulus) && !(p.flags & kFlagStopExit) && t + 1 < cEnd) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
     if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
@@ -1034,11 +1135,15 @@ __device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t 
 }
 
 // Persistent form: every cycle of the launch, regions separated by the
-// bounded grid barrier.
+// bounded grid barrier.  Per cycle: region 0, region 1, (stop exit) the next
+// cycle's inputs, (a retirement) admission; the launch ends early once every
+// queued stream retired or, resident streams with stop exit, every stream
+// stopped.
 template <int SPW, int G>
 __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0, uint32_t nCycles) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) unsigned long long stageMbar[2];
+  __shared__ uint32_t retBits[kMaxSlotWords];
   BlockSmem b;
   if (!setupBlock<G>(p, smem, stageMbar, b)) return;
   const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
@@ -1048,14 +1153,16 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
     applyStimulus<SPW>(p, c0, gtid, gthreads);
     if (!gridSync(p, gen)) return;
   }
-  uint32_t ev = 0;
   const bool slots = (p.flags & kFlagSlots) != 0;
+  uint32_t hint = slots ? __ldcg(p.eventHint + (c0 & 1u)) : 0xFFFFFFFFu;
   for (uint32_t t = c0; t < cEnd; ++t) {
-    const bool event = slots && ev < p.nEvents && __ldg(p.events + ev) == t;
+    const bool scan = slots && mayRetire(p, t, hint);  // the same in every block
+    const uint32_t retCnt = scan ? scanRetiring(p, t, retBits) : 0u;
+    const bool event = retCnt > 0;
 #pragma unroll 1
     for (uint32_t r = 0; r < 2; ++r) {
       const long long tStart = clock64();
-      regionWork<SPW, G>(p, b, t, r, event, ev, cEnd, c0);
+      regionWork<SPW, G>(p, b, t, r, event, retBits, retCnt, cEnd, c0);
       if (!gridSync(p, gen)) return;
       if ((p.flags & kFlagProfile) && threadIdx.x == 0 && t >= c0 + 100 && t < c0 + 200) {
         const long long total = clock64() - tStart;
@@ -1069,18 +1176,22 @@ __global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0
         }
       }
     }
-    if (event) {
-      eventAdmit<SPW>(p, ev, t, gtid, gthreads);
-      ++ev;
-      if (!gridSync(p, gen)) return;
-    }
     if ((p.flags & kFlagStopExit) && (p.flags & kFlagStimulus) && t + 1 < cEnd) {
       applyStimulus<SPW>(p, t + 1, gtid, gthreads);
       if (!gridSync(p, gen)) return;
     }
+    if (event) {
+      eventAdmit<SPW>(p, t, gtid, gthreads);
+      if (!gridSync(p, gen)) return;
+    }
     if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
-    // every block reads the count after the cycle's last barrier: same decision
-    if ((p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) break;
+    // every block reads the words after the cycle's last barrier: same decision
+    if (scan) {
+      hint = __ldcg(p.eventHint + ((t + 1u) & 1u));  // this scan's bound, lowered by the admissions
+      if (__ldcg(p.nDone) >= p.nJobs) break;
+    } else if (!slots && (p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) {
+      break;
+    }
   }
 }
 
@@ -1090,32 +1201,44 @@ template <int SPW, int G>
 __global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k, uint32_t r) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) unsigned long long stageMbar[2];
+  __shared__ uint32_t retBits[kMaxSlotWords];
   // graph state and the error word are written only by earlier launches
   const uint32_t t = __ldcg(p.graphState) + k, cEnd = __ldcg(p.graphState + 2);
   if (t >= cEnd || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
+  const bool slots = (p.flags & kFlagSlots) != 0;
+  // admission words, loaded before the block setup hides their latency
+  const uint32_t adm = !slots ? 0u : r == 0 ? __ldcg(p.eventHint + (t & 1u)) : __ldcg(p.retCount);
   BlockSmem b;
   if (!setupBlock<G>(p, smem, stageMbar, b)) return;
-  const uint32_t ev = __ldcg(p.graphState + 1);
-  const bool event = (p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t;
-  regionWork<SPW, G>(p, b, t, r, event, ev, cEnd, __ldcg(p.graphState + 3));
+  uint32_t retCnt = adm;
+  if (slots && r == 0) {
+    retCnt = 0;
+    if (mayRetire(p, t, adm))
+      retCnt = scanRetiring(p, t, retBits);
+    else if (blockIdx.x == 0 && threadIdx.x == 0)
+      p.eventHint[(t + 1u) & 1u] = adm;  // carried to the next cycle's launch
+  }
+  regionWork<SPW, G>(p, b, t, r, retCnt > 0, retBits, retCnt, cEnd, __ldcg(p.graphState + 3));
 }
 
-// Graph form, after region 1: admission of the cycle's event (one block),
-// cycle bookkeeping.
+// Graph form, after region 1 (and the stop-exit inputs): admission (one
+// block), cycle bookkeeping, the early-exit word.
 template <int SPW>
 __global__ void admitKernel(const KParams p, uint32_t k) {
   const uint32_t t = __ldcg(p.graphState) + k;
-  // graphState[4] (stop exit) is written only here, after the cycle's regions
+  // graphState[4] (exit) is written only here, after the cycle's regions
   if (t >= __ldcg(p.graphState + 2) || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
-  const uint32_t ev = __ldcg(p.graphState + 1);
-  if ((p.flags & kFlagSlots) && ev < p.nEvents && __ldg(p.events + ev) == t) {
-    eventAdmit<SPW>(p, ev, t, threadIdx.x, blockDim.x);
-    __syncthreads();
-    if (threadIdx.x == 0) p.graphState[1] = ev + 1;
-  }
+  const bool slots = (p.flags & kFlagSlots) != 0;
+  const bool event = slots && __ldcg(p.retCount) != 0;
+  if (event) eventAdmit<SPW>(p, t, threadIdx.x, blockDim.x);
+  __syncthreads();
   if (threadIdx.x == 0) {
     if (p.flags & kFlagCountCycles) *p.realCycles += 1;
-    if ((p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) p.graphState[4] = 1;
+    if (slots) {
+      if (event && __ldcg(p.nDone) >= p.nJobs) p.graphState[4] = 1;
+    } else if ((p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) {
+      p.graphState[4] = 1;
+    }
   }
 }
 

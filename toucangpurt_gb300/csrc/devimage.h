@@ -125,20 +125,22 @@ struct KParams {
   uint32_t *slotRetire;       // [slots] global cycle at which it retires (start + length)
   const uint32_t *jobLen;     // [jobs]
   const unsigned long long *jobSeed;  // [jobs]
-  const uint32_t *events;     // [nEvents] global cycles with retirements, increasing
-  const uint32_t *eventBegin; // [nEvents + 1] into eventSlot / eventNext
-  const uint32_t *eventSlot;  // retiring slot
-  const uint32_t *eventNext;  // job stream admitted into it, kNoStream for none
-  uint32_t *retireMask;       // [gpad] nibble masks of the current event's slots
+  const uint32_t *queueOrder; // [jobs] admission order (longest first)
+  uint32_t *queueHead;        // next position in queueOrder
+  uint32_t *queueSnap;        // queueHead when the current cycle's retirements were listed
+  uint32_t *retList;          // [slots] slots retiring in the current cycle, in slot order
+  uint32_t *retCount;         // their number (written every cycle)
+  uint32_t *nDone;            // job streams retired so far
+  uint32_t *eventHint;        // [4] when to scan for retirements (per cycle parity: next length retirement, stop cycle + 1)
+  uint32_t *retireMask;       // [gpad] nibble masks of the current cycle's retiring slots
   unsigned long long *memAcc; // [slots] final memory digests
   unsigned long long *outReg, *outMem, *outRoll;  // [jobs]
   uint32_t *outStop;          // [jobs]
-  uint32_t nEvents, nJobs;
+  uint32_t nJobs;
   // per-micro-partition clock64 profile (kFlagProfileMP), indexed by the id in header word 1
   unsigned long long *mpCycles;
   uint32_t *mpCount;
-  // graph form: cycle counter, event cursor, end cycle and first cycle of the run
-  // graph form: {cycle counter, event cursor, end cycle, first cycle, exit} on the
+  // graph form: {cycle counter, unused, end cycle, first cycle, exit} on the
   // device, so one captured chunk serves every call
   uint32_t *graphState;
   uint32_t *nStopped;         // kFlagStopExit: streams stopped so far
@@ -146,6 +148,7 @@ struct KParams {
 };
 
 constexpr uint32_t kNoStream = 0xFFFFFFFFu;
+constexpr uint32_t kMaxSlotWords = 128;  // admission: at most 4,096 slots (one bit each in shared memory)
 
 enum : uint32_t {
   kFlagStimulus = 1u,   // apply the stimulus before every cycle

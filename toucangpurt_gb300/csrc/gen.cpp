@@ -267,6 +267,20 @@ class PartGen {
   // Value of the latest band (or inputs) for memory-write data etc.
   uint16_t anyRecent() { return pick(uint32_t(bands_.size()), false).slot; }
 
+  // Extra exec level with one micro-partition: a recent value compared with
+  // a constant nibble (EQ window), nonzero in about one cycle in 16.
+  uint16_t rareFlag(std::vector<CGMicroPartInfo> &level) {
+    const uint16_t out = slot(1);
+    CGMicroPartInfo m;
+    m.isLUTPart = true;
+    m.topLevel.push_back({kEq, 0, anyRecent(), uint16_t(1 + rng_.below(15))});
+    ++cnt_.lut;
+    addWriteBack(m.lastLevel, uint8_t(32), out);
+    level.push_back(std::move(m));
+    ++cnt_.mparts;
+    return out;
+  }
+
   void addBandValues(const std::vector<uint16_t> &slots) {
     if (bands_.empty()) {
       for (auto s : slots) inputs_.vals.push_back({s, false});
@@ -700,7 +714,9 @@ void generateDesign(const tgs_gen_config &c, SimDesignInfo &d, SimDebugInfo &s, 
       }
       if (!addrLvl.empty()) part.exec_mParts.push_back(std::move(addrLvl));
       if (stopHere) {
-        uint16_t en = g.anyRecent();
+        std::vector<CGMicroPartInfo> flagLvl;
+        const uint16_t en = c.with_stop == 2 ? g.rareFlag(flagLvl) : g.anyRecent();
+        if (!flagLvl.empty()) part.exec_mParts.push_back(std::move(flagLvl));
         part.ops_last_stop.push_back({en});
         part.ops_last_print.push_back({en, 0});
       }

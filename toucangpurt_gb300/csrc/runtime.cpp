@@ -107,12 +107,12 @@ struct tgs_sim {
   tgs::DBuf<char *> msgPtrs;
   std::vector<tgs::DBuf<char>> msgs;
   tgs::DBuf<uint32_t> ioIds;
-  tgs::DBuf<uint32_t> slotStream, slotStart, slotRetire, jobLen, events, eventBegin, eventSlot, eventNext, retireMask,
-      outStop;
+  tgs::DBuf<uint32_t> slotStream, slotStart, slotRetire, jobLen, queueOrder, retList, retireMask, outStop;
+  tgs::DBuf<uint32_t> admW;  // admission words: queue head, queue snapshot, retire count, done count, scan hints [4]
   tgs::DBuf<unsigned long long> jobSeed, memAcc, outReg, outMem, outRoll;
   tgs::DBuf<uint8_t> stimTable;
   tgs::DBuf<unsigned long long> mpCycles;
-  tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, event cursor, end, first cycle, exit
+  tgs::DBuf<uint32_t> graphState;  // graph form: cycle counter, unused, end, first cycle, exit
   tgs::DBuf<uint32_t> nStopped;    // stop exit: streams stopped
   // signal capture (symbol file signalDebugInfo): probe = one (partition,
   // slot) section; a signal = its sections' probes and widths, most
@@ -293,7 +293,12 @@ void configure(tgs_sim *h) {
     h->model->predictAll(h->img, cost);
     costPtr = &cost;
   }
-  const size_t optin = size_t(h->props.sharedMemPerBlockOptin);
+  // the kernels' static shared memory (barrier words, retirement bitmask)
+  // comes out of the same per-block limit
+  cudaFuncAttributes fa{}, fr{};
+  TGS_CUDA(cudaFuncGetAttributes(&fa, fn));
+  TGS_CUDA(cudaFuncGetAttributes(&fr, regionKernelFor(int(h->spw), G)));
+  const size_t optin = size_t(h->props.sharedMemPerBlockOptin) - std::max(fa.sharedSizeBytes, fr.sharedSizeBytes);
   auto shape = [&](uint32_t stage) {
     h->lc.smem = kLutTablePadded + 2 * size_t(stage) * 4 + vpBytes;
     if (h->lc.smem > optin) return 0;
@@ -1384,9 +1389,9 @@ float runTimed(tgs_sim *h, uint32_t c0, uint32_t n, uint32_t flags) {
   return ms;
 }
 
-// Admission: streams queued onto S resident slots.  The host simulates the
-// queue (every length is known up front): each retirement is an event
-// (global cycle, slot, next stream); the kernel follows the event list.
+// Admission: streams queued onto S resident slots.  The kernel finds each
+// cycle's retirements (length reached or, with stop exit, a stop in the
+// previous cycle) and admits the next queued streams, longest first, in place.
 void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uint32_t flags) {
   const uint32_t n = job->n_streams;
   // default slot count: enough that the queue's work fills the longest
@@ -1401,6 +1406,7 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
                           : uint32_t(std::clamp<uint64_t>((total + longest - 1) / longest, 8, 4096));
   S = std::min(S, n);
   if (S > 1) S = (S + 7) / 8 * 8;
+  if (S > 32u * kMaxSlotWords) throw Error(TGS_ERR_ARG, "queued batches run on at most 4096 slots");
   if (res && (res->final_regs || res->final_mems))
     throw Error(TGS_ERR_ARG, "final_regs / final_mems need every stream resident (slots >= n_streams, equal lengths)");
   if (job->stim && job->stim->table) throw Error(TGS_ERR_ARG, "stimulus tables need every stream resident and equally long");
@@ -1414,46 +1420,35 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
     h->opt.n_streams = S;
     configure(h);
   }
-  // queue simulation: min-heap of (retire cycle, slot).  Streams are admitted
-  // longest first (LPT): every stream's results are independent of when it
-  // runs, and the longest ones no longer start late and run on alone.
+  // Streams are admitted longest first (LPT): every stream's results are
+  // independent of when it runs, and the longest ones no longer start late
+  // and run on alone.
   std::vector<uint32_t> order(n);
   std::iota(order.begin(), order.end(), 0u);
   std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return job->cycles[a] > job->cycles[b]; });
   std::vector<uint32_t> slotStream(S, kNoStream), slotStart(S, 0), slotRetire(S, 0xFFFFFFFFu);
+  // launch length: the queue's end without stops (min-heap of (retire
+  // cycle, slot); a slot freed in cycle t takes its next stream from t + 1).
+  // Shorter streams (stops) never end the queue later: a stream's start
+  // cycle only grows with the lengths before it.
   using E = std::pair<uint64_t, uint32_t>;
   std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
+  uint32_t firstRetire = 0xFFFFFFFFu;
   for (uint32_t s = 0; s < S && s < n; ++s) {
     const uint32_t q = order[s];
     slotStream[s] = q;
     slotRetire[s] = job->cycles[q];
+    firstRetire = std::min(firstRetire, job->cycles[q]);
     pq.push({job->cycles[q], s});
   }
-  std::vector<std::tuple<uint64_t, uint32_t, uint32_t>> evs;  // (cycle, slot, next)
-  uint32_t nextQ = std::min(S, n);
-  while (!pq.empty()) {
+  uint64_t last = 0;
+  for (uint32_t nextQ = std::min(S, n); !pq.empty();) {
     auto [t, s] = pq.top();
     pq.pop();
-    uint32_t qn = kNoStream;
-    if (nextQ < n) {
-      qn = order[nextQ++];
-      pq.push({t + 1 + job->cycles[qn], s});
-    }
-    evs.emplace_back(t, s, qn);
+    last = std::max(last, t);
+    if (nextQ < n) pq.push({t + 1 + job->cycles[order[nextQ++]], s});
   }
-  std::sort(evs.begin(), evs.end());
-  const uint64_t last = std::get<0>(evs.back());
   if (last >= 0xFFFFFFF0ull) throw Error(TGS_ERR_RANGE, "job too long for 32-bit cycle counters");
-  std::vector<uint32_t> events, eventBegin, eventSlot, eventNext;
-  for (size_t i = 0; i < evs.size(); ++i) {
-    if (events.empty() || events.back() != std::get<0>(evs[i])) {
-      events.push_back(uint32_t(std::get<0>(evs[i])));
-      eventBegin.push_back(uint32_t(i));
-    }
-    eventSlot.push_back(std::get<1>(evs[i]));
-    eventNext.push_back(std::get<2>(evs[i]));
-  }
-  eventBegin.push_back(uint32_t(evs.size()));
   std::vector<uint32_t> lens(job->cycles, job->cycles + n);
   std::vector<unsigned long long> seeds(n);
   for (uint32_t q = 0; q < n; ++q) seeds[q] = mix64((job->stim ? job->stim->base_seed : 0) ^ q);
@@ -1467,10 +1462,11 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
   h->slotRetire.upload(slotRetire, st);
   h->jobLen.upload(lens, st);
   h->jobSeed.upload(seeds, st);
-  h->events.upload(events, st);
-  h->eventBegin.upload(eventBegin, st);
-  h->eventSlot.upload(eventSlot, st);
-  h->eventNext.upload(eventNext, st);
+  h->queueOrder.upload(order, st);
+  h->retList.alloc(S);
+  const uint32_t admW[8] = {std::min(S, n), 0, 0, 0, firstRetire, firstRetire, 0xFFFFFFFFu, 0xFFFFFFFFu};
+  h->admW.alloc(8);
+  TGS_CUDA(cudaMemcpyAsync(h->admW.p, admW, sizeof(admW), cudaMemcpyHostToDevice, st));
   h->retireMask.alloc(h->gpad);
   h->memAcc.alloc(S);
   h->outReg.alloc(n);
@@ -1486,17 +1482,19 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
   p.slotRetire = h->slotRetire.p;
   p.jobLen = h->jobLen.p;
   p.jobSeed = h->jobSeed.p;
-  p.events = h->events.p;
-  p.eventBegin = h->eventBegin.p;
-  p.eventSlot = h->eventSlot.p;
-  p.eventNext = h->eventNext.p;
+  p.queueOrder = h->queueOrder.p;
+  p.queueHead = h->admW.p;
+  p.queueSnap = h->admW.p + 1;
+  p.retList = h->retList.p;
+  p.retCount = h->admW.p + 2;
+  p.nDone = h->admW.p + 3;
+  p.eventHint = h->admW.p + 4;
   p.retireMask = h->retireMask.p;
   p.memAcc = h->memAcc.p;
   p.outReg = h->outReg.p;
   p.outMem = h->outMem.p;
   p.outRoll = h->outRoll.p;
   p.outStop = h->outStop.p;
-  p.nEvents = uint32_t(events.size());
   p.nJobs = n;
   p.streamSeed = h->jobSeed.p;
   if (flags & kFlagStimulus) {
@@ -1517,6 +1515,15 @@ void batchAdmission(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res, uin
   if (!res) return;
   res->device_ms = ms;
   res->stream_cycles = total;
+  if (flags & kFlagStopExit) {
+    // a stream that stopped ran through its stop cycle
+    std::vector<uint32_t> stops(n);
+    TGS_CUDA(cudaMemcpyAsync(stops.data(), h->outStop.p, n * 4ull, cudaMemcpyDeviceToHost, st));
+    TGS_CUDA(cudaStreamSynchronize(st));
+    res->stream_cycles = 0;
+    for (uint32_t q = 0; q < n; ++q)
+      res->stream_cycles += stops[q] == 0xFFFFFFFFu ? job->cycles[q] : std::min<uint64_t>(job->cycles[q], stops[q] + 1ull);
+  }
   res->launches = h->lastLaunches;
   if (res->final_reg_digest) TGS_CUDA(cudaMemcpyAsync(res->final_reg_digest, h->outReg.p, n * 8ull, cudaMemcpyDeviceToHost, st));
   if (res->final_mem_digest) TGS_CUDA(cudaMemcpyAsync(res->final_mem_digest, h->outMem.p, n * 8ull, cudaMemcpyDeviceToHost, st));
@@ -1554,7 +1561,6 @@ void batchRun(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res) {
   const bool admission = !equal || (job->slots && job->slots < n);
   if (admission) {
     if (job->flags & TGS_BATCH_CONTINUE) throw Error(TGS_ERR_ARG, "TGS_BATCH_CONTINUE needs every stream resident");
-    if (job->flags & TGS_BATCH_STOP_EXIT) throw Error(TGS_ERR_ARG, "TGS_BATCH_STOP_EXIT needs every stream resident");
     fillParams(h);  // refreshed below after any reconfiguration
     batchAdmission(h, job, res, flags);
     return;
