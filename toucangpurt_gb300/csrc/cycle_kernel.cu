@@ -535,19 +535,30 @@ __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, co
 
 // ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
 // vp, tab: shared addresses of the block's value pool and truth table.
+__device__ __forceinline__ PartDesc loadPart(const PartDesc *pd) {
+  PartDesc d;
+  const uint4 *src = reinterpret_cast<const uint4 *>(pd);
+  uint4 *dst = reinterpret_cast<uint4 *>(&d);
+#pragma unroll
+  for (int i = 0; i < int(sizeof(PartDesc) / 16); ++i) dst[i] = __ldg(src + i);
+  return d;
+}
+
 template <int SPW, int G>
 __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t tab, Stage &st, uint32_t cycle,
                          const uint32_t *retire) {
   const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
-  const PartDesc &d = p.parts[pid];
+  // read-only loads: the descriptor stays valid across the shared-memory
+  // stores (whose memory clobber would otherwise force global reloads)
+  const PartDesc d = loadPart(p.parts + pid);
   const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
-  const uint2 *ld = p.levelDesc + d.schedOff;
+  const uint2 *__restrict__ ld = p.levelDesc + d.schedOff;
   const uint32_t cap = p.stageWords;
   // level descriptors (block offset, words) are loaded two levels ahead so
   // their latency stays off the per-level path
   const uint2 zero2 = make_uint2(0u, 0u);
-  uint2 cur = d.nLevels > 0 ? ld[0] : zero2;
-  uint2 nxt = d.nLevels > 1 ? ld[1] : zero2;
+  uint2 cur = d.nLevels > 0 ? __ldg(ld) : zero2;
+  uint2 nxt = d.nLevels > 1 ? __ldg(ld + 1) : zero2;
   // the first exec level streams in while the level-0 reads run
   if (cap && tid == 0 && d.nLevels) {
     if (cur.y <= cap) stageIssue(st, 0, p.sched + cur.x, cur.y);
@@ -569,7 +580,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
 
   // exec levels: warp w runs the units the schedule gave it
   for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
-    const uint2 after = lv + 2 < d.nLevels ? ld[lv + 2] : zero2;
+    const uint2 after = lv + 2 < d.nLevels ? __ldg(ld + lv + 2) : zero2;
     bool staged = false;
     if (cap) {
       if (lv > 0) __syncthreads();  // staged buffers are reused every second level
