@@ -129,22 +129,32 @@ __device__ __forceinline__ uint32_t lookup<1>(uint32_t tab, uint32_t base, uint3
   return ldsU8(tab + base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
 }
 
+// prmt.b32 in its generic mode: a selector nibble with bit 3 set fills the
+// result byte with the sign bit of the selected byte.  Applied to a byte
+// below 0x80 it gives a zero byte, so one permute yields a zero-extended
+// 12-bit index.
+__device__ __forceinline__ uint32_t prmtIdx(uint32_t bc, uint32_t a, uint32_t sel) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(bc), "r"(a), "r"(sel));
+  return d;
+}
+
 // 8 streams: even streams sit in the low nibble of each byte, odd streams in
 // the high nibble.  (b << 4 | c) of 4 streams is formed per byte lane with
-// masks, the a nibble is paired with it by byte permutes into two 12-bit
-// indices per word, and the 8 table bytes are packed back with permutes.
+// masks; one permute per stream puts its a nibble above it (byte j of the bc
+// and a words, upper half zero), and the 8 table bytes are packed back with
+// permutes.
 template <>
 __device__ __forceinline__ uint32_t lookup<8>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
   const uint32_t t = tab + base;
   const uint32_t bcE = ((B & 0x0F0F0F0Fu) << 4) | (C & 0x0F0F0F0Fu);
   const uint32_t bcO = (B & 0xF0F0F0F0u) | ((C >> 4) & 0x0F0F0F0Fu);
   const uint32_t aE = A & 0x0F0F0F0Fu, aO = (A >> 4) & 0x0F0F0F0Fu;
-  const uint32_t e01 = __byte_perm(bcE, aE, 0x5140), e23 = __byte_perm(bcE, aE, 0x7362);
-  const uint32_t o01 = __byte_perm(bcO, aO, 0x5140), o23 = __byte_perm(bcO, aO, 0x7362);
-  const uint32_t r0 = ldsU8(t + (e01 & 0xFFFFu)), r2 = ldsU8(t + (e01 >> 16));
-  const uint32_t r4 = ldsU8(t + (e23 & 0xFFFFu)), r6 = ldsU8(t + (e23 >> 16));
-  const uint32_t r1 = ldsU8(t + (o01 & 0xFFFFu)), r3 = ldsU8(t + (o01 >> 16));
-  const uint32_t r5 = ldsU8(t + (o23 & 0xFFFFu)), r7 = ldsU8(t + (o23 >> 16));
+  // selector for byte j: result bytes (bc.j, a.j, sign(a.j), sign(a.j))
+  const uint32_t r0 = ldsU8(t + prmtIdx(bcE, aE, 0xCC40u)), r2 = ldsU8(t + prmtIdx(bcE, aE, 0xDD51u));
+  const uint32_t r4 = ldsU8(t + prmtIdx(bcE, aE, 0xEE62u)), r6 = ldsU8(t + prmtIdx(bcE, aE, 0xFF73u));
+  const uint32_t r1 = ldsU8(t + prmtIdx(bcO, aO, 0xCC40u)), r3 = ldsU8(t + prmtIdx(bcO, aO, 0xDD51u));
+  const uint32_t r5 = ldsU8(t + prmtIdx(bcO, aO, 0xEE62u)), r7 = ldsU8(t + prmtIdx(bcO, aO, 0xFF73u));
   const uint32_t lo = __byte_perm(__byte_perm(r0, r2, 0x0040), __byte_perm(r4, r6, 0x0040), 0x5410);
   const uint32_t hi = __byte_perm(__byte_perm(r1, r3, 0x0040), __byte_perm(r5, r7, 0x0040), 0x5410);
   return lo | (hi << 4);
@@ -279,6 +289,10 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
   const Words<SH> wb = mid.at(nMid * W);
   const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;
+  if (hdr & kMPDirectWB) {  // entry l takes lane l's value: no exchange (uniform per record)
+    if (lane < nWB) storeG<H>(vpAddr<G>(vp, res, h0), v);
+    return;
+  }
   uint32_t out[H];
 #pragma unroll
   for (int g = 0; g < H; ++g) {

@@ -21,7 +21,9 @@ namespace tgs {
 // Micro-partition kinds (first header word, bits 0..1).
 enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 
-// Header word: kind | lanes(6) << 2 | nMid(8) << 8 | nWB(6) << 16 | nTop(6) << 24.
+// Header word: kind | lanes(6) << 2 | nMid(8) << 8 | nWB(6) << 16 | nTop(6) << 24
+// | direct write-back << 30 (LUT: write-back entry l takes lane l's result,
+// shuffleId == 32 + l for every entry, so no lane exchange is needed).
 // LUT micro-partition words after the 4-word header (all lane-major):
 //   top:  2 * W words, lane l: [lutIndex | op0 << 16, op1 | op2 << 16] (zero for idle lanes)
 //   mid:  nMid * W words, the reference's packed middle-level op (zero = move of immediate 0)
@@ -32,6 +34,7 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 //   VecOp   (3 words): vec1 | vec2 << 16, vecLength | opName << 16 | isV1V2Const << 24, result
 //   MemRead (4 words): memBase lo, memBase hi | multiWriter << 31, en | addrVec << 16, result
 constexpr uint32_t kMPHeaderWords = 4;
+constexpr uint32_t kMPDirectWB = 1u << 30;
 constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;
 // schedule unit word: record offset (words from the level block) | first
 // group << 24 | (groups - 1) << 27

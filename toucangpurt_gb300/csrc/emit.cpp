@@ -33,10 +33,12 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
   W = std::max<uint32_t>(W, uint32_t(m.lastLevel.size()));
   W = std::max<uint32_t>(W, 1);
   uint32_t nMid = uint32_t(m.middleLevels.size());
+  bool direct = true;
+  for (size_t l = 0; l < m.lastLevel.size(); ++l) direct = direct && m.lastLevel[l].shuffleId == 32 + l;
   align4(net);
   uint32_t off = uint32_t(net.size());
   net.push_back(kMPLut | (W << 2) | (nMid << 8) | (uint32_t(m.lastLevel.size()) << 16) |
-                (uint32_t(m.topLevel.size()) << 24));
+                (uint32_t(m.topLevel.size()) << 24) | (direct ? kMPDirectWB : 0u));
   net.push_back(0);
   net.push_back(0);
   net.push_back(0);
