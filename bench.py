@@ -46,7 +46,9 @@ def args_parse():
     p.add_argument("--streams", type=int, default=0)
     p.add_argument("--groups", type=int, default=0, help="8-stream groups per item (0: the library's default)")
     p.add_argument("--warps", type=int, default=0, help="warps per block (0: the design's typical exec-level width)")
-    p.add_argument("--schedule", default="greedy", choices=["greedy", "learned"])
+    p.add_argument("--schedule", default="auto", choices=["auto", "greedy", "learned"],
+                   help="auto: the learned cost model for batched runs (more than one stream), greedy gate count "
+                        "for the plain single-stream form")
     p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
     p.add_argument("--value-pool", default="compact", choices=["compact", "design"],
                    help="value-pool slots renumbered by live range (default) or as numbered in the design file")
@@ -325,7 +327,8 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
             "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
                                    f"(mean {cyc.mean():.0f}), {s.options()['n_streams']} slots, longest first",
-                       "stream_cycles": int(cyc.sum()), "blocks": st["blocks"], "threads_per_block": st["threads"],
+                       "stream_cycles": int(cyc.sum()), "schedule": a.schedule, "blocks": st["blocks"],
+                       "threads_per_block": st["threads"],
                        "groups_per_item": st["groups_per_item"], **notes},
             "lut_evals_per_s": total / dev_s * st["lut_ops"],
             "e2e": {"value": total / wall_s, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": int(cyc.nbytes),
@@ -378,6 +381,8 @@ def run_gb300(a, rank, ws):
     wd = Path(tempfile.mkdtemp(prefix="tgs_bench_"))
     dp, sp, info = make_design(a.workload, wd, rank, a.override)
     streams = a.streams or workloads.RUNS[a.workload]["streams"]
+    if a.schedule == "auto":
+        a.schedule = "learned" if streams > 1 else "greedy"
     cps = a.cycles_per_step or (200 if a.workload in ("largest", "learned") else 2000)
     schedule = 1 if a.schedule == "learned" else 0
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):

@@ -285,7 +285,8 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
 #pragma unroll
     for (int g = 0; g < H; ++g) v[g] = nv[g];
   }
-  // write-back: shuffleId < 32 immediate, else lane (shuffleId mod 32)
+  // write-back (SimEval.cu:422-447): shuffleId < 32 immediate, else lane
+  // (shuffleId mod 32)
   const Words<SH> wb = mid.at(nMid * W);
   const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;
