@@ -57,7 +57,7 @@ def args_parse():
                    help="cycle loop as one persistent launch or as replayed CUDA-graph chunks (one launch per region)")
     p.add_argument("--slots", type=int, default=0, help="resident slots for queued streams of uneven length")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-sample-cycles", type=int, default=1)
+    p.add_argument("--cpu-sample-cycles", type=int, default=5)
     p.add_argument("--out", default="")
     p.add_argument("--override", action="append", default=[],
                    help="generator field override key=value (e.g. a smaller memory depth for profiling)")
