@@ -49,7 +49,10 @@ def args_parse():
     p.add_argument("--schedule", default="auto", choices=["auto", "greedy", "learned"],
                    help="auto: the learned cost model for batched runs (more than one stream), greedy gate count "
                         "for the plain single-stream form")
-    p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (no shared-memory staging)")
+    p.add_argument("--no-stage", action="store_true", help="read exec levels from global memory (same as --levels global)")
+    p.add_argument("--levels", default="auto", choices=["auto", "resident", "global", "staged"],
+                   help="where blocks read exec levels: resident in shared memory for the launch, staged per level, "
+                        "or global memory (auto: resident when every block still fits on the GPU, else staged)")
     p.add_argument("--value-pool", default="compact", choices=["compact", "design"],
                    help="value-pool slots renumbered by live range (default) or as numbered in the design file")
     p.add_argument("--autotune", action="store_true", help="time the launch configurations first and keep the fastest")
@@ -277,6 +280,15 @@ def run_reference_gpu(a, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def levels_option(a) -> int:
+    """tgs_options.resident_netlist for --levels / --no-stage."""
+    return 2 if a.no_stage else {"auto": 0, "resident": 1, "global": 2, "staged": 3}[a.levels]
+
+
+def exec_levels(st) -> str:
+    return "resident" if st.get("resident_words") else "staged" if st.get("stage_words") else "global"
+
+
 def prepare(a, s):
     """Learned schedule (profile micro-partitions, train the cost model) and
     autotuning, both before the timed region.  Returns notes for `config`."""
@@ -299,7 +311,8 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     from toucangpurt_gb300 import sim, workloads
 
     s = sim.Simulator(n_streams=a.slots or 8, groups_per_item=a.groups, warps_per_block=a.warps,
-                      mode=1 if a.mode == "graph" else 0, value_pool=0 if a.value_pool == "compact" else 1)
+                      resident_netlist=levels_option(a), mode=1 if a.mode == "graph" else 0,
+                      value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
     cyc = workloads.stream_lengths(a.workload, streams, seed=7 + rank)
@@ -327,7 +340,8 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
             "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
                                    f"(mean {cyc.mean():.0f}), {s.options()['n_streams']} slots, longest first",
-                       "stream_cycles": int(cyc.sum()), "schedule": a.schedule, "blocks": st["blocks"],
+                       "stream_cycles": int(cyc.sum()), "schedule": a.schedule, "exec_levels": exec_levels(st),
+                       "blocks": st["blocks"],
                        "threads_per_block": st["threads"],
                        "groups_per_item": st["groups_per_item"], **notes},
             "lut_evals_per_s": total / dev_s * st["lut_ops"],
@@ -388,7 +402,7 @@ def run_gb300(a, rank, ws):
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
         return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
     s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=2 if a.no_stage else 0, mode=1 if a.mode == "graph" else 0,
+                      resident_netlist=levels_option(a), mode=1 if a.mode == "graph" else 0,
                       value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
@@ -438,7 +452,7 @@ def run_gb300(a, rank, ws):
                        "streams": streams, "cycles_per_step": cps, "lut_ops": st["lut_ops"],
                        "partitions": st["partitions"], "schedule": a.schedule, "groups_per_item": st["groups_per_item"],
                        "mode": ["persistent", "graph"][s.options()["mode"]], "value_pool": a.value_pool,
-                       "smem_per_block": st.get("smem_per_block"), **notes,
+                       "smem_per_block": st.get("smem_per_block"), "exec_levels": exec_levels(st), **notes,
                        "threads_per_block": st["threads"], "blocks": st["blocks"],
                        "l2": "working set (memories) larger than L2"},
             "lut_evals_per_s": value * st["lut_ops"],

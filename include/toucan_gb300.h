@@ -67,7 +67,10 @@ typedef struct tgs_options {
   uint32_t mode;             /* TGS_MODE_PERSISTENT or TGS_MODE_GRAPH */
   uint32_t barrier_timeout_ms; /* budget of every device-side wait (default 2000) */
   uint32_t validate;         /* 1 = run the static design checks at init (default 1) */
-  uint32_t resident_netlist; /* 0: stage each exec level into shared memory when it fits (default); 2: read levels from global memory */
+  uint32_t resident_netlist; /* 0 (default): a block's exec levels stay in shared memory for the whole launch when
+                                every block of the launch still fits on the GPU at once, else each level is staged
+                                into shared memory while the previous one runs; 1: resident (TGS_ERR_RESOURCES when
+                                it does not fit); 2: levels read from global memory; 3: staged */
   uint32_t value_pool;       /* 0: renumber value-pool slots by live range (default); 1: the design file's numbering.
                                 Takes effect at the next tgs_init / tgs_init_from_memory */
   uint32_t capture_signals;  /* 1: record every signal of the symbol file each cycle (tgs_read_signal, VCD);
@@ -96,7 +99,8 @@ typedef struct tgs_tune_opts {
 } tgs_tune_opts;
 
 typedef struct tgs_tune_trial {
-  uint32_t groups_per_item, warps_per_block, blocks_per_sm, mode, staged;
+  uint32_t groups_per_item, warps_per_block, blocks_per_sm, mode;
+  uint32_t staged;      /* exec levels: 1 staged per level, 2 resident for the launch, 0 read from global memory */
   uint32_t blocks;      /* grid size of the trial */
   float ms_per_cycle;   /* negative: the configuration does not fit */
 } tgs_tune_trial;
@@ -291,8 +295,9 @@ typedef struct tgs_design_stats {
   uint64_t block_barriers, exec_levels;   /* block barriers kept / exec levels, all partitions */
   double makespan[2];        /* scheduled cost of the slowest block per region */
   uint32_t smem_per_block;   /* dynamic shared memory of a block: table, stage buffers, value pool */
-  uint32_t stage_words;      /* words of one exec-level stage buffer (0: levels read from global memory) */
-  uint32_t reserved[6];
+  uint32_t stage_words;      /* words of one exec-level stage buffer (0: levels resident or read from global memory) */
+  uint32_t resident_words;   /* words of a block's resident exec levels (0: staged or read from global memory) */
+  uint32_t reserved[5];
 } tgs_design_stats;
 int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *out);
 

@@ -64,6 +64,31 @@ def test_batch_parity(designs, name, streams, groups):
     _compare(got, ref)
 
 
+@pytest.mark.parametrize("name", ["small", "wide3op", "mixed", "deep_cones"])
+@pytest.mark.parametrize("levels", [0, 1, 2, 3])  # auto, resident, global, staged
+@pytest.mark.parametrize("mode", [0, 1])  # persistent, graph
+def test_exec_level_sources(designs, name, levels, mode):
+    """Exec levels resident in shared memory for the launch, staged per level,
+    or read from global memory: the same bit-exact results."""
+    dp, sp, info = designs[name]
+    cycles = np.full(24, 30, np.uint32)
+    stim = _stim(info, seed=9)
+    with sim.Simulator(n_streams=24, groups_per_item=2, resident_netlist=levels, mode=mode) as s:
+        s.init(0, dp, sp, False, False)
+        st = s.design_stats()
+        if levels == 1:
+            assert st["resident_words"] > 0 and st["stage_words"] == 0
+        elif levels == 2:
+            assert st["resident_words"] == 0 and st["stage_words"] == 0
+        elif levels == 3:
+            assert st["resident_words"] == 0 and st["stage_words"] > 0
+        got = s.batch_run(cycles, stim, cycle_digests=True)
+        got2 = s.batch_run(cycles, stim, cycle_digests=True)  # a second launch reloads the levels
+    ref = pyoracle.OracleDesign(dp, sp).run(cycles, stim, cycle_digests=True)
+    _compare(got, ref)
+    _compare(got2, ref)
+
+
 @pytest.mark.parametrize("warps", [0, 3, 4, 6, 12, 16, 32])
 def test_warps_per_block(designs, warps):
     dp, sp, info = designs["wide3op"]

@@ -31,7 +31,7 @@ CXX_FLAGS = ["-std=c++20", "-O2", "-fPIC", "-Wall"]
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
 def _stale(obj: Path, src: Path, deps: list[Path]) -> bool:

@@ -97,7 +97,7 @@ class DesignStats(C.Structure):
         ("max_exec_levels", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("groups_per_item", C.c_uint32), ("streams_per_word", C.c_uint32), ("block_barriers", C.c_uint64),
         ("exec_levels", C.c_uint64), ("makespan", C.c_double * 2), ("smem_per_block", C.c_uint32),
-        ("stage_words", C.c_uint32), ("reserved", C.c_uint32 * 6),
+        ("stage_words", C.c_uint32), ("resident_words", C.c_uint32), ("reserved", C.c_uint32 * 5),
     ]
 
 

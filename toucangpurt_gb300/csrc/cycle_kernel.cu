@@ -1,1251 +1,12 @@
-// GB300 (sm_103a) cycle kernel of the Toucan netlist evaluation.
-//
-// Restates the reference device code (src/SimEval.cu:304-1056) for many
-// stimulus streams at once:
-//   * one 32-bit word per value-pool slot carries the nibbles of 8 streams
-//     (SPW = 8; SPW = 1 runs a single stream in nibble 0), so every
-//     __shfl_sync of a micro-partition level moves 8 streams' operands and
-//     the 4,642-entry truth table is indexed once per stream from shared
-//     memory, where a cp.async.bulk copy staged it at kernel start (the
-//     reference reads __constant__ memory with lane-divergent addresses,
-//     SimEval.cu:190,354,411);
-//   * a block evaluates G 8-stream groups of a partition together, giving G
-//     independent dependency chains per warp level (G words per slot in
-//     shared memory, read with one vector load);
-//   * one persistent cooperative launch runs many cycles; regions are
-//     separated by a software grid barrier whose waits are bounded by a
-//     global-timer budget (timeouts set an error word instead of hanging);
-//   * partitions are statically assigned to blocks and micro-partitions to
-//     warps by the host schedule (greedy gate count or learned cost).
-// All mutable device state (registers, exchange, memories) is read with
-// L1-bypassing loads because other blocks write it between barriers.
-#include <cuda_runtime.h>
-
-#include <cstdint>
-#include <cstdio>
-
-#include "devimage.h"
-#include "kernels.h"
+// Small kernels of the cycle loop (graph-form admission, stimulus, cycle
+// counter), state utilities, and the host-side launch wrappers.  The cycle
+// and region kernels are instantiated in kernels_{persistent,region}_
+// {staged,resident}.cu, one translation unit each, so the build compiles
+// them in parallel.
+#include "cycle_kernel.cuh"
 
 namespace tgs {
 namespace {
-
-constexpr uint32_t kFull = 0xFFFFFFFFu;
-
-__device__ __forceinline__ uint32_t rep8(uint32_t v) { return v * 0x11111111u; }
-__device__ __forceinline__ uint32_t nib(uint32_t w, uint32_t k) { return (w >> (4u * k)) & 0xFu; }
-
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ unsigned long long dmix64(unsigned long long z) {
-  z += 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-__device__ __forceinline__ void raiseErr(const KParams &p, uint32_t code, uint32_t a, uint32_t b, uint32_t c) {
-  if (atomicCAS(p.err, 0u, code) == 0u) {
-    p.errInfo[0] = code;
-    p.errInfo[1] = a;
-    p.errInfo[2] = b;
-    p.errInfo[3] = c;
-  }
-}
-
-// ---- shared memory -----------------------------------------------------------
-// Every shared-memory access of the evaluation goes through these helpers with
-// 32-bit shared-window addresses, so the compiler emits shared loads and
-// stores.  (A pointer that may refer to shared or to global memory, such as
-// an exec level that is staged or not, would otherwise compile to generic
-// accesses with 64-bit address arithmetic.)  Stores carry a memory clobber;
-// loads are volatile, so the compiler keeps them in order with the stores.
-__device__ __forceinline__ uint32_t ldsU8(uint32_t a) {
-  uint32_t v;
-  asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
-  return v;
-}
-__device__ __forceinline__ uint32_t ldsU32(uint32_t a) {
-  uint32_t v;
-  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
-  return v;
-}
-__device__ __forceinline__ uint2 ldsV2(uint32_t a) {
-  uint2 v;
-  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
-  return v;
-}
-__device__ __forceinline__ uint4 ldsV4(uint32_t a) {
-  uint4 v;
-  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
-  return v;
-}
-__device__ __forceinline__ void stsU32(uint32_t a, uint32_t v) {
-  asm volatile("st.shared.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
-}
-__device__ __forceinline__ void stsV2(uint32_t a, uint2 v) {
-  asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
-}
-__device__ __forceinline__ void stsV4(uint32_t a, uint4 v) {
-  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
-}
-
-// Words of a level block / micro-partition record: staged in shared memory
-// (SH) or read from the schedule in global memory.
-template <bool SH>
-struct Words {
-  const uint32_t *g;  // global address (SH = false)
-  uint32_t s;         // shared address (SH = true)
-  __device__ __forceinline__ uint32_t operator[](uint32_t i) const {
-    if constexpr (SH) return ldsU32(s + 4u * i);
-    else return __ldg(g + i);
-  }
-  // words i, i + 1 (i even: records are 16-byte aligned)
-  __device__ __forceinline__ uint2 pair(uint32_t i) const {
-    if constexpr (SH) return ldsV2(s + 4u * i);
-    else return __ldg(reinterpret_cast<const uint2 *>(g + i));
-  }
-  __device__ __forceinline__ Words at(uint32_t off) const { return Words{g + off, s + 4u * off}; }
-};
-
-// value-pool slot word (slot, group) of a block's pool at shared address vp
-template <int G>
-__device__ __forceinline__ uint32_t vpAddr(uint32_t vp, uint32_t slot, uint32_t g) {
-  return vp + 4u * (slot * uint32_t(G) + g);
-}
-
-// ---- truth-table lookup ---------------------------------------------------
-// index = lutIndex + (a << 8 | b << 4 | c) per stream (SimEval.cu:353,410);
-// tab = shared address of the staged table.
-template <int SPW>
-__device__ __forceinline__ uint32_t lookup(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C);
-
-template <>
-__device__ __forceinline__ uint32_t lookup<1>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
-  return ldsU8(tab + base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
-}
-
-// prmt.b32 in its generic mode: a selector nibble with bit 3 set fills the
-// result byte with the sign bit of the selected byte.  Applied to a byte
-// below 0x80 it gives a zero byte, so one permute yields a zero-extended
-// 12-bit index.
-__device__ __forceinline__ uint32_t prmtIdx(uint32_t bc, uint32_t a, uint32_t sel) {
-  uint32_t d;
-  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(bc), "r"(a), "r"(sel));
-  return d;
-}
-
-// 8 streams: even streams sit in the low nibble of each byte, odd streams in
-// the high nibble.  (b << 4 | c) of 4 streams is formed per byte lane with
-// masks; one permute per stream puts its a nibble above it (byte j of the bc
-// and a words, upper half zero), and the 8 table bytes are packed back with
-// permutes.
-template <>
-__device__ __forceinline__ uint32_t lookup<8>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
-  const uint32_t t = tab + base;
-  const uint32_t bcE = ((B & 0x0F0F0F0Fu) << 4) | (C & 0x0F0F0F0Fu);
-  const uint32_t bcO = (B & 0xF0F0F0F0u) | ((C >> 4) & 0x0F0F0F0Fu);
-  const uint32_t aE = A & 0x0F0F0F0Fu, aO = (A >> 4) & 0x0F0F0F0Fu;
-  // selector for byte j: result bytes (bc.j, a.j, sign(a.j), sign(a.j))
-  const uint32_t r0 = ldsU8(t + prmtIdx(bcE, aE, 0xCC40u)), r2 = ldsU8(t + prmtIdx(bcE, aE, 0xDD51u));
-  const uint32_t r4 = ldsU8(t + prmtIdx(bcE, aE, 0xEE62u)), r6 = ldsU8(t + prmtIdx(bcE, aE, 0xFF73u));
-  const uint32_t r1 = ldsU8(t + prmtIdx(bcO, aO, 0xCC40u)), r3 = ldsU8(t + prmtIdx(bcO, aO, 0xDD51u));
-  const uint32_t r5 = ldsU8(t + prmtIdx(bcO, aO, 0xEE62u)), r7 = ldsU8(t + prmtIdx(bcO, aO, 0xFF73u));
-  const uint32_t lo = __byte_perm(__byte_perm(r0, r2, 0x0040), __byte_perm(r4, r6, 0x0040), 0x5410);
-  const uint32_t hi = __byte_perm(__byte_perm(r1, r3, 0x0040), __byte_perm(r5, r7, 0x0040), 0x5410);
-  return lo | (hi << 4);
-}
-
-// ---- value-pool words of G groups ----------------------------------------
-template <int G>
-__device__ __forceinline__ void loadG(uint32_t sa, uint32_t (&v)[G]) {
-  if constexpr (G == 8) {
-    const uint4 q = ldsV4(sa), r = ldsV4(sa + 16u);
-    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-    v[4] = r.x; v[5] = r.y; v[6] = r.z; v[7] = r.w;
-  } else if constexpr (G == 4) {
-    const uint4 q = ldsV4(sa);
-    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-  } else if constexpr (G == 2) {
-    const uint2 q = ldsV2(sa);
-    v[0] = q.x; v[1] = q.y;
-  } else {
-    v[0] = ldsU32(sa);
-  }
-}
-
-template <int G>
-__device__ __forceinline__ void storeG(uint32_t sa, const uint32_t (&v)[G]) {
-  if constexpr (G == 8) {
-    stsV4(sa, make_uint4(v[0], v[1], v[2], v[3]));
-    stsV4(sa + 16u, make_uint4(v[4], v[5], v[6], v[7]));
-  } else if constexpr (G == 4) {
-    stsV4(sa, make_uint4(v[0], v[1], v[2], v[3]));
-  } else if constexpr (G == 2) {
-    stsV2(sa, make_uint2(v[0], v[1]));
-  } else {
-    stsU32(sa, v[0]);
-  }
-}
-
-// global (mutable state, L1 bypass) -> value pool
-template <int G>
-__device__ __forceinline__ void copyInG(uint32_t dst, const uint32_t *__restrict__ src) {
-  if constexpr (G == 8) {
-    stsV4(dst, __ldcg(reinterpret_cast<const uint4 *>(src)));
-    stsV4(dst + 16u, __ldcg(reinterpret_cast<const uint4 *>(src) + 1));
-  } else if constexpr (G == 4) {
-    stsV4(dst, __ldcg(reinterpret_cast<const uint4 *>(src)));
-  } else if constexpr (G == 2) {
-    stsV2(dst, __ldcg(reinterpret_cast<const uint2 *>(src)));
-  } else {
-    stsU32(dst, __ldcg(src));
-  }
-}
-
-// value pool -> global
-template <int G>
-__device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t src) {
-  if constexpr (G == 8) {
-    reinterpret_cast<uint4 *>(dst)[0] = ldsV4(src);
-    reinterpret_cast<uint4 *>(dst)[1] = ldsV4(src + 16u);
-  } else if constexpr (G == 4) {
-    *reinterpret_cast<uint4 *>(dst) = ldsV4(src);
-  } else if constexpr (G == 2) {
-    *reinterpret_cast<uint2 *>(dst) = ldsV2(src);
-  } else {
-    *dst = ldsU32(src);
-  }
-}
-
-// ---- micro-partitions (evalSingleMicroPart, SimEval.cu:304-580) -----------
-// One pass of a LUT micro-partition over H stream groups starting at group
-// h0 of the item (value-pool words [slot][G]).
-template <int SPW, int G, int H, bool SH>
-__device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane,
-                                            bool constSlots, uint32_t h0) {
-  const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
-  const Words<SH> top = mp.at(kMPHeaderWords);
-  uint32_t v[H];
-  // top level: operands < 16 are immediates, else value-pool slots
-  if (lane < W) {
-    const uint2 t = top.pair(2u * lane);
-    const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
-    uint32_t A[H], B[H], C[H];
-    if (constSlots) {
-      loadG<H>(vpAddr<G>(vp, a, h0), A);
-      loadG<H>(vpAddr<G>(vp, b, h0), B);
-      loadG<H>(vpAddr<G>(vp, c, h0), C);
-    } else {
-      if (a < 16) {
-#pragma unroll
-        for (int g = 0; g < H; ++g) A[g] = rep8(a);
-      } else {
-        loadG<H>(vpAddr<G>(vp, a, h0), A);
-      }
-      if (b < 16) {
-#pragma unroll
-        for (int g = 0; g < H; ++g) B[g] = rep8(b);
-      } else {
-        loadG<H>(vpAddr<G>(vp, b, h0), B);
-      }
-      if (c < 16) {
-#pragma unroll
-        for (int g = 0; g < H; ++g) C[g] = rep8(c);
-      } else {
-        loadG<H>(vpAddr<G>(vp, c, h0), C);
-      }
-    }
-#pragma unroll
-    for (int g = 0; g < H; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
-  } else {
-#pragma unroll
-    for (int g = 0; g < H; ++g) v[g] = 0;
-  }
-  // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
-  const Words<SH> mid = top.at(2u * W);
-  for (uint32_t m = 0; m < nMid; ++m) {
-    const uint32_t w = lane < W ? mid[m * W + lane] : 0u;
-    const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
-    uint32_t nv[H];
-#pragma unroll
-    for (int g = 0; g < H; ++g) {
-      const uint32_t As = __shfl_sync(kFull, v[g], int(a6 & 31u));
-      const uint32_t Bs = __shfl_sync(kFull, v[g], int(b6 & 31u));
-      const uint32_t Cs = __shfl_sync(kFull, v[g], int(c6 & 31u));
-      const uint32_t A = a6 < 32 ? rep8(a6) : As;
-      const uint32_t B = b6 < 32 ? rep8(b6) : Bs;
-      const uint32_t C = c6 < 32 ? rep8(c6) : Cs;
-      nv[g] = lut ? lookup<SPW>(tab, lut, A, B, C) : C;
-    }
-#pragma unroll
-    for (int g = 0; g < H; ++g) v[g] = nv[g];
-  }
-  // write-back (SimEval.cu:422-447): shuffleId < 32 immediate, else lane
-  // (shuffleId mod 32)
-  const Words<SH> wb = mid.at(nMid * W);
-  const uint32_t wv = lane < nWB ? wb[lane] : 0u;
-  const uint32_t src = wv & 0xFFu, res = wv >> 16;
-  if (hdr & kMPDirectWB) {  // entry l takes lane l's value: no exchange (uniform per record)
-    if (lane < nWB) storeG<H>(vpAddr<G>(vp, res, h0), v);
-    return;
-  }
-  uint32_t out[H];
-#pragma unroll
-  for (int g = 0; g < H; ++g) {
-    const uint32_t x = __shfl_sync(kFull, v[g], int(src & 31u));
-    out[g] = src < 32 ? rep8(src) : x;
-  }
-  if (lane < nWB) storeG<H>(vpAddr<G>(vp, res, h0), out);
-}
-
-// constSlots: value-pool slots 0..15 hold the immediates 0..15 (renumbered
-// pools never use them), so operands are loaded without a branch.  More than
-// 4 groups run as passes of 4 (the record is read once per pass from shared
-// memory; the unit's bookkeeping is paid once).
-template <int SPW, int G, bool SH>
-__device__ __forceinline__ void evalLut(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t tab, uint32_t lane,
-                                        bool constSlots) {
-  constexpr int H = G > 4 ? 4 : G;
-#pragma unroll 1
-  for (uint32_t h0 = 0; h0 < uint32_t(G); h0 += H) evalLutPass<SPW, G, H, SH>(mp, hdr, vp, tab, lane, constSlots, h0);
-}
-
-// Special micro-partitions run on the stream groups [g0, g0 + gn) of the
-// item: the schedule may give the groups of one micro-partition to several
-// warps (a level of one special micro-partition would leave the other warps
-// idle).
-template <int SPW, int G, bool SH>
-__device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d, const Words<SH> mp, uint32_t hdr,
-                                            uint32_t vp, uint32_t lane, uint32_t g0, uint32_t gn) {
-  const uint32_t n = (hdr >> 2) & 63u;
-  if (lane >= n) return;
-  const Words<SH> r = mp.at(kMPHeaderWords + lane * kVecReadWords);
-  const uint32_t w0 = r[0], w1 = r[1], w2 = r[2], w3 = r[3], w4 = r[4];
-  const uint32_t base = w0 & 0xFFFFu, len = w0 >> 16, off = w1 & 0xFFFFu, isConst = (w1 >> 16) & 1u;
-  const uint32_t ix[4] = {w2 & 0xFFFFu, w2 >> 16, w3 & 0xFFFFu, w3 >> 16};
-  const uint32_t outR = w4 & 0xFFFFu, res = w4 >> 16;
-  const uint8_t *cv = p.constVec + d.constOff;
-#pragma unroll 1
-  for (uint32_t g = g0; g < g0 + gn; ++g) {
-    uint32_t I[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : ldsU32(vpAddr<G>(vp, ix[j], g));
-    const uint32_t OR = outR < 16 ? rep8(outR) : ldsU32(vpAddr<G>(vp, outR, g));
-    uint32_t out = 0;
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      const uint32_t o = ((nib(I[0], k) << 12) | (nib(I[1], k) << 8) | (nib(I[2], k) << 4) | nib(I[3], k)) + off;
-      uint32_t val;
-      if (o < len)
-        val = isConst ? uint32_t(__ldg(cv + base + o)) & 15u : nib(ldsU32(vpAddr<G>(vp, base + o, g)), k);
-      else
-        val = nib(OR, k);
-      out |= val << (4 * k);
-    }
-    stsU32(vpAddr<G>(vp, res, g), out);
-  }
-}
-
-// Signed vector arithmetic on up to 31 nibbles per stream (SimEval.cu:482-548):
-// nibble i of the vector sits in slot base + i, sign bit at 4 * len - 1.
-// Work item = (op, group, stream), one per lane: the SPW lanes of one (op,
-// group) hold the streams of one word and merge their result nibbles with
-// shuffles, so no lane runs the streams of a word one after another.
-template <int SPW, int G, bool SH>
-__device__ void evalVecOp(const KParams &p, const PartDesc &d, const Words<SH> mp, uint32_t hdr, uint32_t vp,
-                          uint32_t lane, uint32_t g0, uint32_t gn) {
-  const uint32_t n = (hdr >> 2) & 63u;
-  const uint32_t total = n * gn * SPW;
-  const uint8_t *cv = p.constVec + d.constOff;
-#pragma unroll 1
-  for (uint32_t base = 0; base < total; base += 32) {  // the same trip count in every lane
-    const uint32_t w = base + lane;
-    const bool act = w < total;
-    const uint32_t op = act ? w / (gn * SPW) : 0u;
-    const uint32_t g = g0 + (w / SPW) % gn, k = w % SPW;
-    const Words<SH> r = mp.at(kMPHeaderWords + op * kVecOpWords);
-    const uint32_t w0 = r[0], w1 = r[1], res = r[2];
-    const uint32_t v1 = w0 & 0xFFFFu, v2 = w0 >> 16, len = act ? (w1 & 0xFFFFu) : 0u, opc = (w1 >> 16) & 0xFFu;
-    const uint32_t cf = w1 >> 24;
-    const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
-    const bool isVec = opc <= 2;
-    unsigned __int128 a = 0, b = 0;
-    for (uint32_t i = 0; i < len; ++i) {
-      const uint32_t x = c1 ? (uint32_t(__ldg(cv + v1 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v1 + i, g)), k);
-      const uint32_t y = c2 ? (uint32_t(__ldg(cv + v2 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v2 + i, g)), k);
-      a |= (unsigned __int128)x << (4 * i);
-      b |= (unsigned __int128)y << (4 * i);
-    }
-    unsigned __int128 rv = 0;
-    if (act) {
-      const uint32_t sign = 4 * len - 1;
-      if ((a >> sign) & 1) a |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
-      if ((b >> sign) & 1) b |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
-      const __int128 sa = (__int128)a, sb = (__int128)b;
-      switch (opc) {
-        case 0: rv = a + b; break;
-        case 1: rv = a - b; break;
-        case 2: rv = a * b; break;
-        case 3: rv = sa == sb; break;
-        case 4: rv = sa < sb; break;
-        case 5: rv = sa <= sb; break;
-        default: rv = 0; break;
-      }
-    }
-    // result nibbles: len slots for arithmetic, one slot for a comparison
-    const uint32_t outLen = act ? (isVec ? len : 1u) : 0u;
-    uint32_t maxLen = outLen;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) maxLen = max(maxLen, __shfl_xor_sync(kFull, maxLen, o));
-    for (uint32_t i = 0; i < maxLen; ++i) {
-      uint32_t word = i < outLen ? (uint32_t(rv >> (4 * i)) & 15u) << (4 * k) : 0u;
-#pragma unroll
-      for (int o = 1; o < SPW; o <<= 1) word |= __shfl_xor_sync(kFull, word, o);
-      if (k == 0 && i < outLen) stsU32(vpAddr<G>(vp, (res + i) & 0xFFFFu, g), word);
-    }
-  }
-}
-
-// Memory reads (SimEval.cu:550-575): the loads of the SPW streams of a word
-// are issued together, then merged.
-template <int SPW, int G, bool SH>
-__device__ __forceinline__ void evalMemRead(const KParams &p, const Words<SH> mp, uint32_t hdr, uint32_t vp,
-                                            uint32_t lane, uint32_t gb, uint32_t g0, uint32_t gn) {
-  const uint32_t n = (hdr >> 2) & 63u;
-  if (lane >= n) return;
-  const Words<SH> r = mp.at(kMPHeaderWords + lane * kMemReadWords);
-  const uint32_t lo = r[0], hi = r[1], w2 = r[2], res = r[3];
-  const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
-  const bool multi = (hi >> 31) != 0;
-  const uint32_t en = w2 & 0xFFFFu, av = w2 >> 16;
-  if (en == 0) return;  // immediate 0: neither reads nor writes (SimEval.cu:559-560)
-#pragma unroll 1
-  for (uint32_t g = g0; g < g0 + gn; ++g) {
-    const uint32_t EN = en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g));
-    uint32_t AD[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) AD[j] = ldsU32(vpAddr<G>(vp, av + j, g));
-    uint32_t out = ldsU32(vpAddr<G>(vp, res, g));  // a disabled read leaves the slot as it is
-    uint32_t val[SPW];
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      const uint32_t s = (gb * G + g) * SPW + k;
-      val[k] = 16u;  // no load
-      if (s >= p.nStreams || nib(EN, k) == 0) continue;
-      uint32_t addr = 0;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) addr |= nib(AD[j], k) << (4 * j);
-      if (multi) addr <<= 2;
-      const unsigned long long idx = memBase + addr;
-      if (idx >= p.memPoolSize) {
-        raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
-        continue;
-      }
-      val[k] = __ldcg(p.mems + s * p.memStride + idx) & 15u;
-    }
-#pragma unroll
-    for (int k = 0; k < SPW; ++k)
-      if (val[k] < 16u) out = (out & ~(15u << (4 * k))) | (val[k] << (4 * k));
-    stsU32(vpAddr<G>(vp, res, g), out);
-  }
-}
-
-// ---- exec-level staging ------------------------------------------------------
-// Two shared-memory buffers, one mbarrier each.  Thread 0 issues the bulk copy
-// of level lv + 1 right after the block barrier that opens level lv (so every
-// thread is done with the buffer's previous level); every thread waits on the
-// buffer's phase parity before reading it.  Waits are bounded.
-struct Stage {
-  uint32_t buf0;   // shared address of buffer 0; buffer b at buf0 + b * bytes
-  uint32_t bytes;  // bytes of one buffer
-  uint32_t mb0;    // shared address of mbarrier 0; mbarrier b at mb0 + 8 * b
-  uint32_t phase;  // bit b: phase parity of buffer b's next completion
-};
-
-__device__ __forceinline__ void stageIssue(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words) {
-  const uint32_t bytes = words * 4u;
-  const uint32_t dst = st.buf0 + b * st.bytes, mb = st.mb0 + 8u * b;
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(mb)
-               : "memory");
-}
-
-// A waiting thread is suspended by the hardware (up to this many ns per try)
-// instead of spinning: no issue slots are spent on the wait.
-constexpr uint32_t kStageSuspendNs = 20000;
-
-__device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t b) {
-  const uint32_t parity = (st.phase >> b) & 1u, mb = st.mb0 + 8u * b;
-  uint32_t done = 0;
-  unsigned long long t0 = 0;
-  for (uint32_t spin = 0; !done; ++spin) {
-    asm volatile(
-        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, P;\n\t}"
-        : "=r"(done)
-        : "r"(mb), "r"(parity), "r"(kStageSuspendNs)
-        : "memory");
-    if (!done) {
-      if (spin == 0) t0 = gtimer();
-      else if (gtimer() - t0 > p.timeoutNs) {
-        raiseErr(p, kErrTimeout, blockIdx.x, 0xFFFFFFFEu, b);
-        return false;
-      }
-    }
-  }
-  st.phase ^= 1u << b;
-  return true;
-}
-
-// The units a warp runs in one exec level (block = the level's words).
-template <int SPW, int G, bool SH>
-__device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, const Words<SH> blk, uint32_t vp,
-                                         uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
-  const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
-  const Words<SH> units = blk.at(2 + NW);
-  if (!(p.flags & kFlagProfileMP)) {
-    for (uint32_t u = ub; u < ue; ++u) {
-      // unit word: record offset | first group << 24 | (groups - 1) << 27
-      const uint32_t uw = units[u];
-      const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
-      const uint32_t hdr = mp[0];
-      if ((hdr & 3u) == kMPLut) {
-        evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0);  // always every group
-      } else {
-        const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
-        if ((hdr & 3u) == kMPVecRead) evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
-        else if ((hdr & 3u) == kMPVecOp) evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
-        else evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn);
-      }
-      __syncwarp();
-    }
-    return;
-  }
-  // the same with clock64 around every unit (cost-model samples)
-  for (uint32_t u = ub; u < ue; ++u) {
-    const uint32_t uw = units[u];
-    const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
-    const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
-    const uint32_t hdr = mp[0];
-    const long long tm = clock64();
-    switch (hdr & 3u) {
-      case kMPLut: evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0); break;
-      case kMPVecRead: evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
-      case kMPVecOp: evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn); break;
-      default: evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn); break;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      const uint32_t id = mp[1];
-      atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
-      atomicAdd(p.mpCount + id, gn);  // groups evaluated
-    }
-  }
-}
-
-// ---- one partition for G groups (evalEachPartition, SimEval.cu:765-864) ---
-// vp, tab: shared addresses of the block's value pool and truth table.
-__device__ __forceinline__ PartDesc loadPart(const PartDesc *pd) {
-  PartDesc d;
-  const uint4 *src = reinterpret_cast<const uint4 *>(pd);
-  uint4 *dst = reinterpret_cast<uint4 *>(&d);
-#pragma unroll
-  for (int i = 0; i < int(sizeof(PartDesc) / 16); ++i) dst[i] = __ldg(src + i);
-  return d;
-}
-
-template <int SPW, int G>
-__device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t tab, Stage &st, uint32_t cycle,
-                         const uint32_t *retire) {
-  const uint32_t pid = item & 0xFFFFFu, gb = item >> 20;
-  // read-only loads: the descriptor stays valid across the shared-memory
-  // stores (whose memory clobber would otherwise force global reloads)
-  const PartDesc d = loadPart(p.parts + pid);
-  const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31u, warp = tid >> 5, NW = nthr >> 5;
-  const uint2 *__restrict__ ld = p.levelDesc + d.schedOff;
-  const uint32_t cap = p.stageWords;
-  // level descriptors (block offset, words) are loaded two levels ahead so
-  // their latency stays off the per-level path
-  const uint2 zero2 = make_uint2(0u, 0u);
-  uint2 cur = d.nLevels > 0 ? __ldg(ld) : zero2;
-  uint2 nxt = d.nLevels > 1 ? __ldg(ld + 1) : zero2;
-  // the first exec level streams in while the level-0 reads run
-  if (cap && tid == 0 && d.nLevels) {
-    if (cur.y <= cap) stageIssue(st, 0, p.sched + cur.x, cur.y);
-  }
-
-  // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
-  {
-    const uint32_t n = d.l0Count;
-    const uint32_t *src = p.net + d.l0Off;
-    const uint32_t *dst = src + n;
-    const uint32_t *pool = d.l0Exchange ? p.exg : p.regs;
-    for (uint32_t i = tid; i < n; i += nthr) {
-      const uint32_t s = __ldg(src + i);
-      const uint32_t r = (__ldg(dst + (i >> 1)) >> ((i & 1u) * 16)) & 0xFFFFu;
-      copyInG<G>(vpAddr<G>(vp, r, 0), pool + size_t(s) * p.gpad + gb * G);
-    }
-  }
-  __syncthreads();
-
-  // exec levels: warp w runs the units the schedule gave it
-  for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
-    const uint2 after = lv + 2 < d.nLevels ? __ldg(ld + lv + 2) : zero2;
-    bool staged = false;
-    if (cap) {
-      if (lv > 0) __syncthreads();  // staged buffers are reused every second level
-      if (tid == 0 && lv + 1 < d.nLevels) {
-        if (nxt.y <= cap) stageIssue(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y);
-      }
-      // on a (never expected) wait timeout the level is read from global
-      // memory instead: same words, uniform control flow, and the error word
-      // ends the launch at the next grid barrier
-      staged = cur.y <= cap && stageWait(p, st, lv & 1u);
-    } else if (lv > 0 && (__ldg(p.sched + cur.x) & 1u)) {
-      __syncthreads();
-    }
-    if (staged)
-      runLevel<SPW, G, true>(p, d, Words<true>{nullptr, st.buf0 + (lv & 1u) * st.bytes}, vp, tab, lane, warp, NW, gb);
-    else
-      runLevel<SPW, G, false>(p, d, Words<false>{p.sched + cur.x, 0u}, vp, tab, lane, warp, NW, gb);
-    cur = nxt;
-    nxt = after;
-  }
-  __syncthreads();
-
-  // signal capture: the value-pool slots the symbol file names as signals
-  if (p.probeBuf)
-    for (uint32_t i = tid; i < d.probeCount * G; i += nthr) {
-      const uint32_t pi = i / G, g = i % G;
-      const uint32_t slot = __ldg(p.net + d.probeOff + 2 * pi), idx = __ldg(p.net + d.probeOff + 2 * pi + 1);
-      p.probeBuf[size_t(idx) * p.gpad + gb * G + g] = ldsU32(vpAddr<G>(vp, slot, g));
-    }
-
-  // last level (evalLastLevel / evalLastLevelExgWrite, SimEval.cu:625-761)
-  // masks of streams retiring this cycle (admission): their registers take
-  // the initial values, their memory writes / prints / stops are dropped
-  uint32_t rm[G];
-#pragma unroll
-  for (int g = 0; g < G; ++g) rm[g] = retire ? __ldcg(retire + gb * G + g) : 0u;
-  // stop exit: streams stopped in an earlier cycle keep their state; their
-  // register words are rewritten with the values they hold (a stopped stream
-  // that retires now takes the initial values instead)
-  const bool stopExit = (p.flags & kFlagStopExit) != 0;
-  uint32_t fm[G], xm[G];
-#pragma unroll
-  for (int g = 0; g < G; ++g) {
-    fm[g] = 0;
-    if (stopExit) {
-#pragma unroll
-      for (int k = 0; k < SPW; ++k) {
-        const uint32_t s = (gb * G + g) * SPW + k;
-        if (s < p.nStreams && __ldcg(p.stopCycle + s) < cycle) fm[g] |= 15u << (4 * k);
-      }
-      fm[g] &= ~rm[g];
-    }
-    xm[g] = rm[g] | fm[g];  // streams whose writes are dropped this cycle
-  }
-  if (d.copyKind == 1 && (stopExit || retire)) {
-    for (uint32_t i = tid; i < d.copySlots; i += nthr) {
-      uint32_t init = 0;
-      if (retire) {
-        const uint32_t iv = p.initRegs[d.copyDst + i];
-        init = SPW == 8 ? rep8(iv) : iv;
-      }
-      uint32_t *dst = p.regs + size_t(d.copyDst + i) * p.gpad + gb * G;
-      uint32_t w[G];
-      loadG<G>(vpAddr<G>(vp, d.copySrc + i, 0), w);
-#pragma unroll
-      for (int g = 0; g < G; ++g) {
-        uint32_t v = (w[g] & ~xm[g]) | (init & rm[g]);
-        if (stopExit) v |= __ldcg(dst + g) & fm[g];
-        dst[g] = v;
-      }
-    }
-  } else if (d.copyKind) {
-    uint32_t *pool = d.copyKind == 1 ? p.regs : p.exg;
-    for (uint32_t i = tid; i < d.copySlots; i += nthr)
-      copyOutG<G>(pool + size_t(d.copyDst + i) * p.gpad + gb * G, vpAddr<G>(vp, d.copySrc + i, 0));
-  }
-  if (d.copyKind != 2) {
-    for (uint32_t i = tid; i < d.memWCount * G; i += nthr) {
-      const uint32_t opi = i / G, g = i % G;
-      const uint32_t *r = p.net + d.memWOff + 4 * opi;
-      const uint32_t lo = __ldg(r), hi = __ldg(r + 1), w2 = __ldg(r + 2), en = __ldg(r + 3);
-      const unsigned long long memBase = (unsigned long long)lo | ((unsigned long long)(hi & 0x7FFFFFFFu) << 32);
-      const bool multi = (hi >> 31) != 0;
-      const uint32_t av = w2 & 0xFFFFu, dat = w2 >> 16;
-      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
-      const uint32_t DAT = dat < 16 ? rep8(dat) : ldsU32(vpAddr<G>(vp, dat, g));
-      uint32_t AD[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) AD[j] = ldsU32(vpAddr<G>(vp, av + j, g));
-#pragma unroll
-      for (int k = 0; k < SPW; ++k) {
-        const uint32_t s = (gb * G + g) * SPW + k;
-        if (s >= p.nStreams || nib(EN, k) == 0) continue;
-        uint32_t addr = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) addr |= nib(AD[j], k) << (4 * j);
-        if (multi) addr <<= 2;
-        const unsigned long long idx = memBase + addr;
-        if (idx >= p.memPoolSize) {
-          raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
-          continue;
-        }
-        p.mems[s * p.memStride + idx] = uint8_t(nib(DAT, k));
-      }
-    }
-    if (p.enablePrint) {
-      for (uint32_t i = tid; i < d.printCount * G; i += nthr) {
-        const uint32_t w = __ldg(p.net + d.printOff + i / G), g = i % G;
-        const uint32_t en = w & 0xFFFFu, msg = w >> 16;
-        const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
-        for (int k = 0; k < SPW; ++k) {
-          const uint32_t s = (gb * G + g) * SPW + k;
-          if (s < p.nStreams && nib(EN, k) != 0 && msg < p.nPrintMsgs) printf("%s", p.printMsgs[msg]);
-        }
-      }
-    }
-    for (uint32_t i = tid; i < d.stopCount * G; i += nthr) {
-      const uint32_t opi = i / G, g = i % G;
-      const uint32_t sw = __ldg(p.net + d.stopOff + opi), en = sw & 0xFFFFu;
-      const uint32_t EN = (en < 16 ? rep8(en) : ldsU32(vpAddr<G>(vp, en, g))) & ~xm[g];
-      for (int k = 0; k < SPW; ++k) {
-        const uint32_t s = (gb * G + g) * SPW + k;
-        if (s >= p.nStreams || nib(EN, k) == 0) continue;
-        if (atomicExch(p.stop + s, 1u) == 0u) {
-          p.stopCycle[s] = cycle;
-          if (stopExit) {
-            atomicAdd(p.nStopped, 1u);
-            if (p.flags & kFlagSlots) p.eventHint[2u + (cycle & 1u)] = cycle + 1u;  // a retirement next cycle
-          }
-          if (p.printDiag) {
-            printf("Toucan first stop: partition=%u op=%u enable_slot=%u value=%u\n", pid, opi, sw >> 16, nib(EN, k));
-            for (uint32_t q = 0; q < d.printCount; ++q) {
-              const uint32_t w = __ldg(p.net + d.printOff + q);
-              if ((w & 0xFFFFu) == en && (w >> 16) < p.nPrintMsgs)
-                printf("Stop-associated message (literal): %s\n", p.printMsgs[w >> 16]);
-            }
-          }
-        }
-      }
-    }
-  }
-  // the next item reuses the value pool
-  __syncthreads();
-}
-
-// ---- stimulus / digests ------------------------------------------------------
-// Value of input `inp` of slot s for global cycle `cycle`; false when the slot
-// takes no input that cycle (idle, past its stream's end, or a padding slot).
-__device__ __forceinline__ bool stimValue(const KParams &p, uint32_t s, uint32_t cycle, uint32_t inp, uint32_t cur,
-                                          uint32_t mask, uint32_t tog, uint32_t &v) {
-  uint32_t lc;
-  unsigned long long seed;
-  if (s >= p.nStreams) return false;  // padding slot of the last group
-  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;  // frozen after its stop
-  if (p.flags & kFlagSlots) {
-    const uint32_t q = __ldcg(p.slotStream + s);
-    if (q == kNoStream || cycle >= __ldcg(p.slotRetire + s)) return false;
-    lc = cycle - __ldcg(p.slotStart + s);
-    seed = __ldg(p.jobSeed + q);
-  } else {
-    lc = cycle;
-    seed = __ldg(p.streamSeed + s);
-    if (p.stimTable) {
-      v = __ldg(p.stimTable + (size_t(cycle - p.stimTableC0) * p.nStim + inp) * p.nStreams + s) & 15u;
-      return true;
-    }
-  }
-  const unsigned long long h = dmix64(seed ^ dmix64((unsigned long long)lc << 32 | inp));
-  if (tog == 0)
-    v = uint32_t(h) & mask;
-  else
-    v = (h >> 48) < tog ? cur ^ mask : cur;
-  return true;
-}
-
-template <int SPW>
-__device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
-  const uint32_t total = p.nStim * p.gpad;
-  for (uint32_t i = gtid; i < total; i += gthreads) {
-    const uint32_t inp = i / p.gpad, g = i % p.gpad;
-    const uint32_t reg = __ldg(p.stimReg + inp);
-    const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
-    const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
-    uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
-    const uint32_t w = __ldcg(wp);
-    uint32_t nw = 0;
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      const uint32_t cur = nib(w, k);
-      uint32_t v = cur;
-      stimValue(p, g * SPW + k, cycle, inp, cur, mask, tog, v);
-      nw |= v << (4 * k);
-    }
-    *wp = nw;
-  }
-}
-
-// A slot retires in cycle t when its stream's last cycle was t - 1: the
-// stream's length was reached, or (stop exit) it executed a stop op in t - 1.
-__device__ __forceinline__ bool retiringAt(const KParams &p, uint32_t s, uint32_t t) {
-  if (__ldcg(p.slotStream + s) == kNoStream) return false;
-  if (__ldcg(p.slotRetire + s) == t) return true;
-  if (!(p.flags & kFlagStopExit)) return false;
-  const uint32_t sc = __ldcg(p.stopCycle + s);
-  return sc != 0xFFFFFFFFu && sc + 1u == t;
-}
-
-// Streams whose register digest this cycle contributes: every active stream
-// with per-cycle digests, else (admission) only the streams retiring now.
-__device__ __forceinline__ bool digestStream(const KParams &p, uint32_t s, uint32_t cycle) {
-  if (s >= p.nStreams) return false;
-  if (p.flags & kFlagSlots) {
-    if (__ldcg(p.slotStream + s) == kNoStream) return false;
-    if (retiringAt(p, s, cycle)) return true;  // the retiring stream's final register digest
-  }
-  if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) return false;  // frozen
-  return !(p.flags & kFlagSlots) || (p.flags & kFlagDigest);
-}
-
-// Per-cycle register digest: sum over i of mix64(i << 8 | nibble), per stream.
-template <int SPW>
-__device__ void digestSlice(const KParams &p, uint32_t cycle) {
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
-  const uint32_t chunks = (p.regSlots + 255) / 256;
-  const uint32_t units = chunks * p.gpad;
-  for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
-    const uint32_t g = u % p.gpad, ch = u / p.gpad;
-    bool want[SPW];
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      want[k] = digestStream(p, g * SPW + k, cycle);
-      any |= want[k];
-    }
-    if (!any) continue;
-    unsigned long long acc[SPW];
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) acc[k] = 0;
-    const uint32_t end = min(p.regSlots, ch * 256 + 256);
-    for (uint32_t i = ch * 256 + lane; i < end; i += 32) {
-      const uint32_t w = __ldcg(p.regs + size_t(i) * p.gpad + g);
-#pragma unroll
-      for (int k = 0; k < SPW; ++k) acc[k] += dmix64((unsigned long long)i << 8 | nib(w, k));
-    }
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      unsigned long long a = acc[k];
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-      if (lane == 0 && want[k]) atomicAdd(p.digAcc + g * SPW + k, a);
-    }
-  }
-}
-
-__device__ void foldDigest(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
-  for (uint32_t s = gtid; s < p.nStreams; s += gthreads) {
-    uint32_t q = s, lc = cycle - p.cycBase;
-    if ((p.flags & kFlagStopExit) && __ldcg(p.stopCycle + s) < cycle) continue;
-    if (p.flags & kFlagSlots) {
-      q = __ldcg(p.slotStream + s);
-      if (q == kNoStream || retiringAt(p, s, cycle)) continue;  // retiring: kept for the admin phase
-      lc = cycle - __ldcg(p.slotStart + s);
-    }
-    const unsigned long long dg = __ldcg(p.digAcc + s);
-    p.digAcc[s] = 0;
-    p.roll[s] = dmix64(p.roll[s] + dg);
-    if (p.cycDig && lc < p.cycStride) p.cycDig[size_t(q) * p.cycStride + lc] = dg;
-  }
-}
-
-// ---- admission events --------------------------------------------------------
-// Retirements are found on the device: a stream may end at its length or, with
-// stop exit, at its stop op, so no list is fixed in advance.  Queued streams
-// are admitted in the order of queueOrder (longest first).
-//
-// A cycle is scanned only when a slot may retire in it.  eventHint words:
-// [t & 1] a lower bound of the next length retirement as of cycle t (a scan
-// in cycle t writes the bound for t + 1, admissions lower it; the graph form
-// carries it from cycle to cycle, the persistent form keeps it in a register
-// between scans); [2 + (c & 1)] = c + 1 when a stream stopped in cycle c.
-// The words read in cycle t are written only in earlier cycles, so every block
-// takes the same decision.
-__device__ __forceinline__ bool mayRetire(const KParams &p, uint32_t t, uint32_t hint) {
-  return t >= hint || ((p.flags & kFlagStopExit) && __ldcg(p.eventHint + 2u + ((t - 1u) & 1u)) == t);
-}
-
-// Every block builds the same bitmask of the slots retiring in cycle t (the
-// state it reads was last written before this cycle's first region) and gets
-// their number; block 0 writes the next length-retirement bound.
-__device__ uint32_t scanRetiring(const KParams &p, uint32_t t, uint32_t *bits) {
-  __shared__ uint32_t count, nextMin;
-  const bool stopExit = (p.flags & kFlagStopExit) != 0;
-  if (threadIdx.x == 0) {
-    count = 0;
-    nextMin = 0xFFFFFFFFu;
-  }
-  __syncthreads();
-  const uint32_t nw = (p.nStreams + 31u) / 32u, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t NW = blockDim.x >> 5;
-  uint32_t c = 0, mn = 0xFFFFFFFFu;
-  for (uint32_t w = warp; w < nw; w += NW) {
-    const uint32_t s = w * 32u + lane;
-    bool ret = false;
-    if (s < p.nStreams) {
-      const uint32_t q = __ldcg(p.slotStream + s), re = __ldcg(p.slotRetire + s), sc = __ldcg(p.stopCycle + s);
-      if (q != kNoStream) {
-        ret = re == t || (stopExit && sc != 0xFFFFFFFFu && sc + 1u == t);
-        if (!ret) mn = min(mn, re);
-      }
-    }
-    const uint32_t m = __ballot_sync(kFull, ret);
-    if (lane == 0) {
-      bits[w] = m;
-      c += __popc(m);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, o));
-  if (lane == 0) {
-    if (c) atomicAdd(&count, c);
-    if (blockIdx.x == 0) atomicMin(&nextMin, mn);
-  }
-  __syncthreads();
-  if (blockIdx.x == 0 && threadIdx.x == 0) p.eventHint[(t + 1u) & 1u] = nextMin;
-  return count;
-}
-
-// The j-th set bit of the bitmask.
-__device__ __forceinline__ uint32_t nthRetiring(const uint32_t *bits, uint32_t nw, uint32_t j) {
-  for (uint32_t w = 0; w < nw; ++w) {
-    uint32_t m = bits[w];
-    const uint32_t c = __popc(m);
-    if (j < c) {
-      for (; j; --j) m &= m - 1u;
-      return w * 32u + uint32_t(__ffs(int(m))) - 1u;
-    }
-    j -= c;
-  }
-  return 0xFFFFFFFFu;
-}
-
-// Region 0 of cycle t: list the retiring slots (block 0: the list, the count,
-// the queue position and the retire masks) and digest their memories.
-template <int SPW>
-__device__ void eventRegion0(const KParams &p, const uint32_t *bits, uint32_t cnt) {
-  const uint32_t nw = (p.nStreams + 31u) / 32u;
-  if (blockIdx.x == 0) {
-    if (threadIdx.x == 0) {
-      *p.retCount = cnt;
-      if (cnt) {
-        uint32_t j = 0;
-        for (uint32_t w = 0; w < nw; ++w)
-          for (uint32_t m = bits[w]; m; m &= m - 1u) p.retList[j++] = w * 32u + uint32_t(__ffs(int(m))) - 1u;
-        *p.queueSnap = __ldcg(p.queueHead);
-      }
-    }
-    for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) {
-      const uint32_t s = nthRetiring(bits, nw, j);
-      atomicOr(p.retireMask + s / SPW, 15u << (4 * (s % SPW)));
-    }
-  }
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
-  const uint32_t chunk = 8192, chunks = (p.memPoolSize + chunk - 1) / chunk;
-  const uint32_t units = cnt * chunks;
-  for (uint32_t u = blockIdx.x * NW + warp; u < units; u += p.nBlocks * NW) {
-    const uint32_t s = nthRetiring(bits, nw, u / chunks), ch = u % chunks;
-    const uint8_t *m = p.mems + s * p.memStride;
-    unsigned long long a = 0;
-    const uint32_t end = min(p.memPoolSize, (ch + 1) * chunk);
-    for (uint32_t i = ch * chunk + lane; i < end; i += 32) a += dmix64((unsigned long long)i << 8 | __ldcg(m + i));
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-    if (lane == 0) atomicAdd(p.memAcc + s, a);
-  }
-}
-
-// Region 1 of a retire cycle: reset the retiring slots' memories (their
-// memory writes are dropped this cycle).
-__device__ void eventRegion1(const KParams &p, uint32_t gtid, uint32_t gthreads) {
-  const uint32_t cnt = __ldcg(p.retCount);
-  const uint32_t vecs = uint32_t((p.memPoolSize + 15ull) / 16);
-  const size_t total = size_t(cnt) * vecs;
-  for (size_t i = gtid; i < total; i += gthreads) {
-    const uint32_t s = __ldcg(p.retList + uint32_t(i / vecs));
-    const size_t v = i % vecs;
-    reinterpret_cast<uint4 *>(p.mems + s * p.memStride)[v] = __ldg(reinterpret_cast<const uint4 *>(p.initMems) + v);
-  }
-}
-
-// After the region-1 barrier: publish the retired streams' results and admit
-// the next queued streams, in queue order, into the listed slots (with their
-// cycle-0 inputs).
-template <int SPW>
-__device__ void eventAdmit(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
-  const uint32_t cnt = __ldcg(p.retCount), head = __ldcg(p.queueSnap);
-  for (uint32_t j = gtid; j < cnt; j += gthreads) {
-    const uint32_t s = __ldcg(p.retList + j);
-    const uint32_t qn = head + j < p.nJobs ? __ldg(p.queueOrder + head + j) : kNoStream;
-    const uint32_t q = __ldcg(p.slotStream + s), start = __ldcg(p.slotStart + s);
-    p.outReg[q] = __ldcg(p.digAcc + s);
-    p.outMem[q] = __ldcg(p.memAcc + s);
-    p.outRoll[q] = __ldcg(p.roll + s);
-    const uint32_t sc = __ldcg(p.stopCycle + s);
-    p.outStop[q] = sc == 0xFFFFFFFFu ? sc : sc - start;
-    atomicAdd(p.nDone, 1u);
-    p.digAcc[s] = 0;
-    p.memAcc[s] = 0;
-    p.roll[s] = 0;
-    p.stop[s] = 0;
-    p.stopCycle[s] = 0xFFFFFFFFu;
-    const uint32_t g = s / SPW, k = s % SPW;
-    atomicAnd(p.retireMask + g, ~(15u << (4 * k)));
-    if (qn == kNoStream) {
-      p.slotStream[s] = kNoStream;
-      continue;
-    }
-    p.slotStream[s] = qn;
-    p.slotStart[s] = cycle + 1;
-    p.slotRetire[s] = cycle + 1 + __ldg(p.jobLen + qn);
-    atomicMin(p.eventHint + ((cycle + 1u) & 1u), cycle + 1 + __ldg(p.jobLen + qn));
-    // primary inputs restart from the initial register values
-    for (uint32_t inp = 0; inp < p.nStim; ++inp) {
-      const uint32_t reg = __ldg(p.stimReg + inp);
-      const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
-      const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
-      const uint32_t cur = p.initRegs[reg] & 15u;
-      uint32_t v = cur;
-      const unsigned long long h = dmix64(__ldg(p.jobSeed + qn) ^ dmix64((unsigned long long)0 << 32 | inp));
-      if (tog == 0)
-        v = uint32_t(h) & mask;
-      else
-        v = (h >> 48) < tog ? cur ^ mask : cur;
-      uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
-      atomicAnd(wp, ~(15u << (4 * k)));
-      atomicOr(wp, v << (4 * k));
-    }
-  }
-  if (gtid == 0) *p.queueHead = min(head + cnt, p.nJobs);
-}
-
-// ---- grid barrier (bounded) --------------------------------------------------
-__device__ __forceinline__ bool gridSync(const KParams &p, uint32_t &gen) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    const uint32_t target = gen + 1;
-    __threadfence();
-    const uint32_t arrived = atomicAdd(p.barrier, 1u);
-    if (arrived == p.nBlocks - 1) {
-      atomicExch(p.barrier, 0u);
-      __threadfence();
-      atomicExch(p.barrier + 1, target);
-    } else {
-      const unsigned long long t0 = gtimer();
-      volatile uint32_t *vg = p.barrier + 1;
-      volatile uint32_t *ve = p.err;
-      while (int32_t(*vg - target) < 0) {
-        if (*ve != 0u) { ok = 0; break; }
-        if (gtimer() - t0 > p.timeoutNs) {
-          raiseErr(p, kErrTimeout, blockIdx.x, target, 0);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    gen = target;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
-// Stages the truth table into shared memory with one bulk async copy.
-__device__ bool stageTable(const KParams &p, uint8_t *tab) {
-  __shared__ __align__(8) unsigned long long mbar;
-  const uint32_t mb = uint32_t(__cvta_generic_to_shared(&mbar));
-  const uint32_t dst = uint32_t(__cvta_generic_to_shared(tab));
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(kLutTablePadded) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(p.lutTable), "r"(kLutTablePadded), "r"(mb)
-                 : "memory");
-  }
-  uint32_t done = 0;
-  const unsigned long long t0 = gtimer();
-  while (!done) {
-    asm volatile(
-        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], 0;\n\tselp.u32 %0, 1, 0, P;\n\t}"
-        : "=r"(done)
-        : "r"(mb)
-        : "memory");
-    if (!done && gtimer() - t0 > p.timeoutNs) {
-      raiseErr(p, kErrTimeout, blockIdx.x, 0xFFFFFFFFu, 1);
-      return false;
-    }
-  }
-  return true;
-}
-
-// ---- kernels -----------------------------------------------------------------
-// Shared-memory layout of a block: truth table, two exec-level stage buffers,
-// value pool.  Returns false when staging the table timed out.
-struct BlockSmem {
-  uint32_t tab;  // shared address of the truth table
-  uint32_t vp;   // shared address of the value pool
-  Stage st;
-};
-
-template <int G>
-__device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsigned long long *stageMbar, BlockSmem &b) {
-  const uint32_t base = uint32_t(__cvta_generic_to_shared(smem));
-  b.tab = base;
-  b.st.buf0 = base + kLutTablePadded;
-  b.st.bytes = p.stageWords * 4u;
-  b.st.mb0 = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
-  b.st.phase = 0;
-  b.vp = b.st.buf0 + 2u * b.st.bytes;
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b.st.mb0 + 8u) : "memory");
-  }
-  if (p.constSlots)  // immediates 0..15 in value-pool slots 0..15
-    for (uint32_t i = threadIdx.x; i < 16u * G; i += blockDim.x) stsU32(b.vp + 4u * i, rep8(i / G));
-  const bool staged = stageTable(p, smem);
-  __syncthreads();
-  return staged;
-}
-
-// One region of cycle t for this block: its items, then the region's side
-// work (digests and retiring-stream capture in region 0; memory reset of
-// retiring streams, next cycle's inputs and digest folding in region 1).
-template <int SPW, int G>
-__device__ void regionWork(const KParams &p, BlockSmem &b, uint32_t t, uint32_t r, bool event, const uint32_t *retBits,
-                           uint32_t retCnt, uint32_t cEnd, uint32_t c0) {
-  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
-  const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
-  const uint32_t i0 = __ldg(ib + blockIdx.x), i1 = __ldg(ib + blockIdx.x + 1);
-  for (uint32_t i = i0; i < i1; ++i) {
-    const long long tk = clock64();
-    const uint32_t item = __ldg(p.items + i);
-    evalItem<SPW, G>(p, item, b.vp, b.tab, b.st, t, (event && r == 1) ? p.retireMask : nullptr);
-    // per-partition clock64 profile (SimEval.cu:894-983): running mean of the
-    // useful ticks over cycles [100, 200) of a launch, group block 0
-    if ((p.flags & kFlagProfile) && threadIdx.x == 0 && (item >> 20) == 0 && t >= c0 + 100 && t < c0 + 200) {
-      const uint32_t pid = item & 0xFFFFFu, pc = t - c0 - 100;
-      p.profUseful[pid] = (p.profUseful[pid] * pc + (clock64() - tk)) / (pc + 1);
-    }
-  }
-  if (r == 0) {
-    if ((p.flags & kFlagDigest) || event) digestSlice<SPW>(p, t);
-    if (p.flags & kFlagSlots) eventRegion0<SPW>(p, retBits, retCnt);  // the cycle's list, also when empty
-  } else {
-    if (event) eventRegion1(p, gtid, gthreads);
-    // (stop exit: applied after the region barrier, when every stop of the cycle is known)
-    if ((p.flags & kFlagStimulus) && !(p.flags & kFlagStopExit) && t + 1 < cEnd) applyStimulus<SPW>(p, t + 1, gtid, gthreads);
-    if (p.flags & kFlagDigest) foldDigest(p, t, gtid, gthreads);
-  }
-}
-
-// Persistent form: every cycle of the launch, regions separated by the
-// bounded grid barrier.  Per cycle: region 0, region 1, (stop exit) the next
-// cycle's inputs, (a retirement) admission; the launch ends early once every
-// queued stream retired or, resident streams with stop exit, every stream
-// stopped.
-template <int SPW, int G>
-__global__ void __launch_bounds__(1024) cycleKernel(const KParams p, uint32_t c0, uint32_t nCycles) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) unsigned long long stageMbar[2];
-  __shared__ uint32_t retBits[kMaxSlotWords];
-  BlockSmem b;
-  if (!setupBlock<G>(p, smem, stageMbar, b)) return;
-  const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = p.nBlocks * blockDim.x;
-  const uint32_t cEnd = c0 + nCycles;
-  uint32_t gen = 0;
-  if (p.flags & kFlagStimulus) {
-    applyStimulus<SPW>(p, c0, gtid, gthreads);
-    if (!gridSync(p, gen)) return;
-  }
-  const bool slots = (p.flags & kFlagSlots) != 0;
-  uint32_t hint = slots ? __ldcg(p.eventHint + (c0 & 1u)) : 0xFFFFFFFFu;
-  for (uint32_t t = c0; t < cEnd; ++t) {
-    const bool scan = slots && mayRetire(p, t, hint);  // the same in every block
-    const uint32_t retCnt = scan ? scanRetiring(p, t, retBits) : 0u;
-    const bool event = retCnt > 0;
-#pragma unroll 1
-    for (uint32_t r = 0; r < 2; ++r) {
-      const long long tStart = clock64();
-      regionWork<SPW, G>(p, b, t, r, event, retBits, retCnt, cEnd, c0);
-      if (!gridSync(p, gen)) return;
-      if ((p.flags & kFlagProfile) && threadIdx.x == 0 && t >= c0 + 100 && t < c0 + 200) {
-        const long long total = clock64() - tStart;
-        const uint32_t pc = t - c0 - 100;
-        const uint32_t *ib = p.itemBegin + r * (p.nBlocks + 1);
-        for (uint32_t i = __ldg(ib + blockIdx.x); i < __ldg(ib + blockIdx.x + 1); ++i) {
-          const uint32_t item = __ldg(p.items + i);
-          if ((item >> 20) != 0) continue;
-          const uint32_t pid = item & 0xFFFFFu;
-          p.profTotal[pid] = (p.profTotal[pid] * pc + total) / (pc + 1);
-        }
-      }
-    }
-    if ((p.flags & kFlagStopExit) && (p.flags & kFlagStimulus) && t + 1 < cEnd) {
-      applyStimulus<SPW>(p, t + 1, gtid, gthreads);
-      if (!gridSync(p, gen)) return;
-    }
-    if (event) {
-      eventAdmit<SPW>(p, t, gtid, gthreads);
-      if (!gridSync(p, gen)) return;
-    }
-    if ((p.flags & kFlagCountCycles) && blockIdx.x == 0 && threadIdx.x == 0) *p.realCycles += 1;
-    // every block reads the words after the cycle's last barrier: same decision
-    if (scan) {
-      hint = __ldcg(p.eventHint + ((t + 1u) & 1u));  // this scan's bound, lowered by the admissions
-      if (__ldcg(p.nDone) >= p.nJobs) break;
-    } else if (!slots && (p.flags & kFlagStopExit) && __ldcg(p.nStopped) >= p.nStreams) {
-      break;
-    }
-  }
-}
-
-// Graph form: one launch per region, kernel boundaries instead of the grid
-// barrier; cycle = device counter + k so one captured chunk is replayed.
-template <int SPW, int G>
-__global__ void __launch_bounds__(1024) regionKernel(const KParams p, uint32_t k, uint32_t r) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) unsigned long long stageMbar[2];
-  __shared__ uint32_t retBits[kMaxSlotWords];
-  // graph state and the error word are written only by earlier launches
-  const uint32_t t = __ldcg(p.graphState) + k, cEnd = __ldcg(p.graphState + 2);
-  if (t >= cEnd || __ldcg(p.graphState + 4) || __ldcg(p.err)) return;
-  const bool slots = (p.flags & kFlagSlots) != 0;
-  // admission words, loaded before the block setup hides their latency
-  const uint32_t adm = !slots ? 0u : r == 0 ? __ldcg(p.eventHint + (t & 1u)) : __ldcg(p.retCount);
-  BlockSmem b;
-  if (!setupBlock<G>(p, smem, stageMbar, b)) return;
-  uint32_t retCnt = adm;
-  if (slots && r == 0) {
-    retCnt = 0;
-    if (mayRetire(p, t, adm))
-      retCnt = scanRetiring(p, t, retBits);
-    else if (blockIdx.x == 0 && threadIdx.x == 0)
-      p.eventHint[(t + 1u) & 1u] = adm;  // carried to the next cycle's launch
-  }
-  regionWork<SPW, G>(p, b, t, r, retCnt > 0, retBits, retCnt, cEnd, __ldcg(p.graphState + 3));
-}
 
 // Graph form, after region 1 (and the stop-exit inputs): admission (one
 // block), cycle bookkeeping, the early-exit word.
@@ -1353,41 +114,28 @@ __global__ void pokeRegsKernel(uint32_t *__restrict__ regs, uint32_t gpad, uint3
   }
 }
 
-template <int SPW, int G>
-void *cycleKernelPtr() {
-  return reinterpret_cast<void *>(&cycleKernel<SPW, G>);
-}
-
 }  // namespace
 
-void *cycleKernelFor(int spw, int G) {
-  if (spw == 1) return cycleKernelPtr<1, 1>();
-  if (G == 8) return cycleKernelPtr<8, 8>();
-  if (G == 4) return cycleKernelPtr<8, 4>();
-  if (G == 2) return cycleKernelPtr<8, 2>();
-  return cycleKernelPtr<8, 1>();
+void *cycleKernelFor(int spw, int G, bool resident) {
+  return resident ? cycleKernelResident(spw, G) : cycleKernelStaged(spw, G);
 }
 
 cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint32_t n) {
-  void *fn = cycleKernelFor(c.spw, c.G);
+  void *fn = cycleKernelFor(c.spw, c.G, c.res);
   KParams pp = p;
   void *args[] = {&pp, &c0, &n};
   return cudaLaunchCooperativeKernel(fn, dim3(c.blocks), dim3(c.threads), args, c.smem, c.stream);
 }
 
-void *regionKernelFor(int spw, int G) {
-  if (spw == 1) return reinterpret_cast<void *>(&regionKernel<1, 1>);
-  if (G == 8) return reinterpret_cast<void *>(&regionKernel<8, 8>);
-  if (G == 4) return reinterpret_cast<void *>(&regionKernel<8, 4>);
-  if (G == 2) return reinterpret_cast<void *>(&regionKernel<8, 2>);
-  return reinterpret_cast<void *>(&regionKernel<8, 1>);
+void *regionKernelFor(int spw, int G, bool resident) {
+  return resident ? regionKernelResident(spw, G) : regionKernelStaged(spw, G);
 }
 
 // Enqueues one chunk of k cycles in graph form on the stream (captured by
 // the caller): per cycle region 0, region 1 and (admission / cycle count)
 // the admit kernel; then the cycle counter advance.
 cudaError_t enqueueGraphChunk(const LaunchCfg &c, const KParams &p, uint32_t k, bool admit) {
-  void *fn = regionKernelFor(c.spw, c.G);
+  void *fn = regionKernelFor(c.spw, c.G, c.res);
   KParams pp = p;
   for (uint32_t i = 0; i < k; ++i) {
     for (uint32_t r = 0; r < 2; ++r) {

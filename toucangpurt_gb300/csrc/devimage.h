@@ -68,7 +68,10 @@ static_assert(sizeof(PartDesc) == 96, "PartDesc size");
 // records, once each, in warp order].  KParams::levelDesc
 // holds (block offset, block words) per level; PartDesc::schedOff indexes
 // the partition's first level there.  A block is staged into shared memory
-// with one bulk async copy while the previous level computes.
+// with one bulk async copy while the previous level computes, or, when the
+// levels of every partition a block evaluates fit in its shared memory, they
+// are copied there once per launch and stay resident (a partition's level
+// blocks are contiguous in KParams::sched).
 
 // Kernel parameters (passed by value).
 struct KParams {
@@ -77,7 +80,10 @@ struct KParams {
   const uint2 *levelDesc;     // (block offset, words) per partition level
   uint32_t stageWords;        // capacity of each shared-memory stage buffer (0 = no staging)
   uint32_t constSlots;        // 1: value-pool slots 0..15 are free (renumbered pools) and hold the immediates
-  uint32_t stagePad;
+  uint32_t resWords;          // words of a block's resident exec levels (0: staged or read from global memory)
+  const uint32_t *itemRes;    // per item: word offset of its partition's levels in the block's resident area
+  const uint32_t *resCopy;    // (schedule word, words, resident word) per copy: a partition's levels, contiguous
+  const uint32_t *resCopyBegin;  // [2][nBlocks + 1] prefix offsets into resCopy (triples) per region and block
   const PartDesc *parts;
   const uint8_t *constVec;
   const uint8_t *lutTable;    // 4642 entries, padded to 4656

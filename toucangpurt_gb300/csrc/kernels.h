@@ -11,13 +11,19 @@ namespace tgs {
 
 struct LaunchCfg {
   int spw = 1, G = 1;
+  bool res = false;  // exec levels resident in shared memory for the launch
   uint32_t blocks = 1, threads = 256;
   size_t smem = 0;
   cudaStream_t stream = nullptr;
 };
 
-void *cycleKernelFor(int spw, int G);
-void *regionKernelFor(int spw, int G);
+void *cycleKernelFor(int spw, int G, bool resident);
+void *regionKernelFor(int spw, int G, bool resident);
+// instantiated one per translation unit (kernels_*.cu)
+void *cycleKernelStaged(int spw, int G);
+void *cycleKernelResident(int spw, int G);
+void *regionKernelStaged(int spw, int G);
+void *regionKernelResident(int spw, int G);
 cudaError_t enqueueGraphChunk(const LaunchCfg &c, const KParams &p, uint32_t k, bool admit);
 cudaError_t launchStimulus(int spw, const KParams &p, uint32_t cycle, cudaStream_t st);
 cudaError_t launchCycles(const LaunchCfg &c, const KParams &p, uint32_t c0, uint32_t n);

@@ -95,9 +95,11 @@ struct tgs_sim {
   // launch configuration
   tgs::LaunchCfg lc;
   uint32_t spw = 1, groups = 1, gpad = 1, nStreams = 1, regSlots = 4, exgSlots = 4, stageWords = 0;
+  uint32_t resWords = 0;  // words of a block's resident exec levels (0: staged or global)
   unsigned long long memStride = 16;
 
   // device memory
+  tgs::DBuf<uint32_t> itemRes, resCopy, resCopyBegin;  // resident exec levels (see configure)
   tgs::DBuf<uint32_t> net, schedW, levelDesc, items, itemBegin, regs, exg, stop, stopCycle, err, errInfo, barrier, realCycles, stimReg;
   tgs::DBuf<tgs::PartDesc> parts;
   tgs::DBuf<uint8_t> constVec, lutTable, mems, initRegs, initMems, stimBits;
@@ -186,6 +188,10 @@ void fillParams(tgs_sim *h) {
   p.sched = h->schedW.p;
   p.levelDesc = reinterpret_cast<const uint2 *>(h->levelDesc.p);
   p.stageWords = h->stageWords;
+  p.resWords = h->resWords;
+  p.itemRes = h->itemRes.p;
+  p.resCopy = h->resCopy.p;
+  p.resCopyBegin = h->resCopyBegin.p;
   p.constSlots = h->img.renumbered ? 1u : 0u;
   p.parts = h->parts.p;
   p.constVec = h->constVec.p;
@@ -278,7 +284,9 @@ void configure(tgs_sim *h) {
   h->lc.G = G;
   h->lc.threads = NW * 32;
   h->lc.stream = h->stream;
-  void *fn = cycleKernelFor(int(h->spw), G);
+  h->lc.res = false;
+  void *fn = cycleKernelFor(int(h->spw), G, false);
+  void *fnRegion = regionKernelFor(int(h->spw), G, false);
   const size_t vpBytes = size_t(h->img.maxVpSlots) * size_t(G) * 4;
   const uint32_t nGB = h->gpad / uint32_t(G);
   size_t maxItems = 1;
@@ -297,14 +305,13 @@ void configure(tgs_sim *h) {
   // comes out of the same per-block limit
   cudaFuncAttributes fa{}, fr{};
   TGS_CUDA(cudaFuncGetAttributes(&fa, fn));
-  TGS_CUDA(cudaFuncGetAttributes(&fr, regionKernelFor(int(h->spw), G)));
+  TGS_CUDA(cudaFuncGetAttributes(&fr, fnRegion));
   const size_t optin = size_t(h->props.sharedMemPerBlockOptin) - std::max(fa.sharedSizeBytes, fr.sharedSizeBytes);
   auto shape = [&](uint32_t stage) {
     h->lc.smem = kLutTablePadded + 2 * size_t(stage) * 4 + vpBytes;
     if (h->lc.smem > optin) return 0;
     TGS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
-    TGS_CUDA(cudaFuncSetAttribute(regionKernelFor(int(h->spw), G), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(h->lc.smem)));
+    TGS_CUDA(cudaFuncSetAttribute(fnRegion, cudaFuncAttributeMaxDynamicSharedMemorySize, int(h->lc.smem)));
     int perSM = 0;
     TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, int(h->lc.threads), h->lc.smem));
     if (o.blocks_per_sm) perSM = std::min<int>(perSM, int(o.blocks_per_sm));
@@ -335,6 +342,73 @@ void configure(tgs_sim *h) {
   h->stageWords = stage;
   h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
   buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, h->lc.blocks, nGB, h->sched);
+
+  // Resident exec levels: the levels of every partition a block evaluates
+  // (both regions, one contiguous range of the schedule per partition) are
+  // copied into the block's shared memory once per launch, replacing one
+  // bulk copy per level whose latency a short level cannot hide.  Chosen
+  // when every block of the grid still fits on the GPU at once.
+  h->resWords = 0;
+  {
+    const uint32_t B = h->lc.blocks;
+    std::vector<uint32_t> itemRes(h->sched.items.size(), 0), resCopy, resBegin(2 * (B + 1), 0), at(B, 0);
+    std::vector<uint32_t> placedAt(h->design.parts.size(), UINT32_MAX);
+    for (uint32_t r = 0; r < 2; ++r)
+      for (uint32_t b = 0; b <= B; ++b) {
+        resBegin[r * (B + 1) + b] = uint32_t(resCopy.size() / 3);
+        if (b == B) break;
+        const uint32_t i0 = h->sched.itemBegin[r * (B + 1) + b], i1 = h->sched.itemBegin[r * (B + 1) + b + 1];
+        std::vector<uint32_t> placed;
+        for (uint32_t i = i0; i < i1; ++i) {
+          const uint32_t pid = h->sched.items[i] & 0xFFFFFu;
+          const PartDesc &pd = h->img.parts[pid];
+          if (placedAt[pid] == UINT32_MAX && pd.nLevels) {
+            const uint32_t first = h->sched.levelDesc[2 * pd.schedOff];
+            const uint32_t last = pd.schedOff + pd.nLevels - 1;
+            const uint32_t end = (h->sched.levelDesc[2 * last] + h->sched.levelDesc[2 * last + 1] + 3u) & ~3u;
+            placedAt[pid] = at[b];
+            resCopy.insert(resCopy.end(), {first, end - first, at[b]});
+            at[b] += end - first;
+            placed.push_back(pid);
+          }
+          itemRes[i] = placedAt[pid] == UINT32_MAX ? 0u : placedAt[pid];
+        }
+        for (uint32_t pid : placed) placedAt[pid] = UINT32_MAX;
+      }
+    const uint32_t words = B ? *std::max_element(at.begin(), at.end()) : 0u;
+    const uint32_t want = o.resident_netlist;  // 0 auto, 1 resident, 2 global, 3 staged
+    if ((want == 0 || want == 1) && words) {
+      const size_t smemRes = kLutTablePadded + vpBytes + size_t(words) * 4;
+      int perSMRes = 0;
+      void *fnRes = cycleKernelFor(int(h->spw), G, true), *fnRegionRes = regionKernelFor(int(h->spw), G, true);
+      cudaFuncAttributes ra{}, rr{};
+      TGS_CUDA(cudaFuncGetAttributes(&ra, fnRes));
+      TGS_CUDA(cudaFuncGetAttributes(&rr, fnRegionRes));
+      const size_t optinRes = size_t(h->props.sharedMemPerBlockOptin) - std::max(ra.sharedSizeBytes, rr.sharedSizeBytes);
+      if (smemRes <= optinRes) {
+        TGS_CUDA(cudaFuncSetAttribute(fnRes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemRes)));
+        TGS_CUDA(cudaFuncSetAttribute(fnRegionRes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemRes)));
+        TGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSMRes, fnRes, int(h->lc.threads), smemRes));
+        if (o.blocks_per_sm) perSMRes = std::min<int>(perSMRes, int(o.blocks_per_sm));
+      }
+      if (perSMRes > 0 && size_t(perSMRes) * h->props.multiProcessorCount >= B) {
+        h->resWords = words;
+        h->stageWords = 0;
+        h->lc.smem = smemRes;
+        h->lc.res = true;
+        h->itemRes.upload(itemRes, h->stream);
+        h->resCopy.upload(resCopy, h->stream);
+        h->resCopyBegin.upload(resBegin, h->stream);
+      } else {
+        if (want == 1)
+          throw Error(TGS_ERR_RESOURCES, "resident exec levels need " + std::to_string(smemRes) +
+                                             " B of shared memory per block for " + std::to_string(B) + " blocks");
+        shape(stage);  // back to the staged (or global) size
+      }
+    } else if (want == 1) {
+      throw Error(TGS_ERR_RESOURCES, "resident exec levels: the blocks have no levels to keep");
+    }
+  }
   h->parts.upload(h->img.parts, h->stream);
   h->schedW.upload(h->sched.words, h->stream);
   h->levelDesc.upload(h->sched.levelDesc, h->stream);
@@ -858,7 +932,7 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
             if (fits && h->lc.blocks == lastBlocks) continue;  // same grid as the previous trial
             if (fits) lastBlocks = h->lc.blocks;
             tr.blocks = fits ? h->lc.blocks : 0;
-            tr.staged = fits && h->stageWords ? 1u : 0u;
+            tr.staged = !fits ? 0u : h->resWords ? 2u : h->stageWords ? 1u : 0u;
             for (uint32_t mode = 0; mode < 2; ++mode) {
               if (!(modes & (1u << mode))) continue;
               tr.mode = mode;
@@ -886,7 +960,7 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
     h->opt.warps_per_block = win.warps_per_block;
     h->opt.blocks_per_sm = win.blocks_per_sm;
     h->opt.mode = win.mode;
-    h->opt.resident_netlist = win.staged ? 0u : (base.resident_netlist == 2 || o.try_unstaged ? 2u : 0u);
+    h->opt.resident_netlist = win.staged ? 0u : 2u;  // the default picks resident / staged as in the trial
     configure(h);
     resetState(h);
     h->cycleCnt = 0;
@@ -1709,6 +1783,7 @@ extern "C" int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *o) {
     o->makespan[1] = h->sched.makespan[1];
     o->smem_per_block = uint32_t(h->lc.smem);
     o->stage_words = h->stageWords;
+    o->resident_words = h->resWords;
   });
 }
 
