@@ -1084,31 +1084,32 @@ __device__ void eventAdmit(const KParams &p, uint32_t cycle, uint32_t gtid, uint
 __device__ __forceinline__ bool gridSync(const KParams &p, uint32_t &gen) {
   __shared__ int ok;
   __syncthreads();
+  // a one-block grid (a single stream of a small design): the block barrier
+  // already orders the block's global writes before its later reads
+  if (gridDim.x == 1) return true;
   if (threadIdx.x == 0) {
     ok = 1;
-    const uint32_t target = gen + 1;
+    // arrivals only ever add to the counter (zeroed before each launch):
+    // barrier g of the launch is complete once it reaches g * blocks, so the
+    // last block to arrive has nothing more to write (wrap-safe compare)
+    const uint32_t target = (gen + 1u) * gridDim.x;
     __threadfence();
-    const uint32_t arrived = atomicAdd(p.barrier, 1u);
-    if (arrived == p.nBlocks - 1) {
-      atomicExch(p.barrier, 0u);
-      __threadfence();
-      atomicExch(p.barrier + 1, target);
-    } else {
+    const uint32_t arrived = atomicAdd(p.barrier, 1u) + 1u;
+    if (arrived != target) {
       const unsigned long long t0 = gtimer();
-      volatile uint32_t *vg = p.barrier + 1;
+      volatile uint32_t *vc = p.barrier;
       volatile uint32_t *ve = p.err;
-      while (int32_t(*vg - target) < 0) {
+      while (int32_t(*vc - target) < 0) {
         if (*ve != 0u) { ok = 0; break; }
         if (gtimer() - t0 > p.timeoutNs) {
-          raiseErr(p, kErrTimeout, blockIdx.x, target, 0);
+          raiseErr(p, kErrTimeout, blockIdx.x, gen + 1u, 0);
           ok = 0;
           break;
         }
-        __nanosleep(64);
       }
     }
     __threadfence();
-    gen = target;
+    gen += 1u;
   }
   __syncthreads();
   return ok != 0;

@@ -98,7 +98,7 @@ struct KParams {
   uint32_t *stopCycle;        // [nStreams] first stop cycle
   uint32_t *err;              // device error word (kErr*)
   uint32_t *errInfo;          // [4] detail of the first error
-  uint32_t *barrier;          // [2]: arrival counter, generation
+  uint32_t *barrier;          // [2]: grid-barrier arrival counter (zeroed per launch), unused word
   uint32_t *realCycles;
   unsigned long long *digAcc; // [nStreams] per-cycle digest accumulators
   unsigned long long *roll;   // [nStreams] rolling digests
