@@ -339,17 +339,17 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
 #pragma unroll
     for (int j = 0; j < 4; ++j) I[j] = ix[j] < 16 ? rep8(ix[j]) : ldsU32(vpAddr<G>(vp, ix[j], g));
     const uint32_t OR = outR < 16 ? rep8(outR) : ldsU32(vpAddr<G>(vp, outR, g));
-    uint32_t out = 0;
+    // the SPW reads of a word are issued before any is used
+    uint32_t raw[SPW];
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
       const uint32_t o = ((nib(I[0], k) << 12) | (nib(I[1], k) << 8) | (nib(I[2], k) << 4) | nib(I[3], k)) + off;
-      uint32_t val;
-      if (o < len)
-        val = isConst ? uint32_t(__ldg(cv + base + o)) & 15u : nib(ldsU32(vpAddr<G>(vp, base + o, g)), k);
-      else
-        val = nib(OR, k);
-      out |= val << (4 * k);
+      if (o < len) raw[k] = isConst ? uint32_t(__ldg(cv + base + o)) : nib(ldsU32(vpAddr<G>(vp, base + o, g)), k);
+      else raw[k] = nib(OR, k);
     }
+    uint32_t out = 0;
+#pragma unroll
+    for (int k = 0; k < SPW; ++k) out |= (raw[k] & 15u) << (4 * k);
     stsU32(vpAddr<G>(vp, res, g), out);
   }
 }
@@ -434,26 +434,31 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const Words<SH> mp
 #pragma unroll
     for (int j = 0; j < 8; ++j) AD[j] = ldsU32(vpAddr<G>(vp, av + j, g));
     uint32_t out = ldsU32(vpAddr<G>(vp, res, g));  // a disabled read leaves the slot as it is
+    // every stream's load is issued (predicated) before any is used, and an
+    // out-of-range address is reported after them, so the SPW loads of a
+    // word overlap instead of waiting one after another
     uint32_t val[SPW];
+    uint32_t badK = SPW;
+    unsigned long long badIdx = 0;
 #pragma unroll
     for (int k = 0; k < SPW; ++k) {
       const uint32_t s = (gb * G + g) * SPW + k;
-      val[k] = 16u;  // no load
-      if (s >= p.nStreams || nib(EN, k) == 0) continue;
       uint32_t addr = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) addr |= nib(AD[j], k) << (4 * j);
       if (multi) addr <<= 2;
       const unsigned long long idx = memBase + addr;
-      if (idx >= p.memPoolSize) {
-        raiseErr(p, kErrMemRange, uint32_t(idx), uint32_t(idx >> 32), s);
-        continue;
+      const bool on = s < p.nStreams && nib(EN, k) != 0, ok = on && idx < p.memPoolSize;
+      if (on && !ok && badK == SPW) {
+        badK = uint32_t(k);
+        badIdx = idx;
       }
-      val[k] = __ldcg(p.mems + s * p.memStride + idx) & 15u;
+      val[k] = ok ? uint32_t(__ldcg(p.mems + s * p.memStride + idx)) : 0xFFu;  // 0xFF: no load
     }
+    if (badK != SPW) raiseErr(p, kErrMemRange, uint32_t(badIdx), uint32_t(badIdx >> 32), (gb * G + g) * SPW + badK);
 #pragma unroll
     for (int k = 0; k < SPW; ++k)
-      if (val[k] < 16u) out = (out & ~(15u << (4 * k))) | (val[k] << (4 * k));
+      if (val[k] != 0xFFu) out = (out & ~(15u << (4 * k))) | ((val[k] & 15u) << (4 * k));
     stsU32(vpAddr<G>(vp, res, g), out);
   }
 }
