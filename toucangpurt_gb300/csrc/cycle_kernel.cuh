@@ -826,6 +826,33 @@ __device__ __forceinline__ bool stimValue(const KParams &p, uint32_t s, uint32_t
 template <int SPW>
 __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, uint32_t gthreads) {
   const uint32_t total = p.nStim * p.gpad;
+  if constexpr (SPW == 8) {
+    // eight lanes per register word, one stream each: the streams' slot
+    // reads and hashes run side by side instead of one after another, and
+    // the nibbles merge by shuffles within the lane octet.  Whole warps
+    // iterate together (gthreads and the bound are multiples of 32).
+    const uint32_t k = gtid & 7u, lanes = (total * 8u + 31u) & ~31u;
+    for (uint32_t t = gtid; t < lanes; t += gthreads) {
+      const uint32_t i = t >> 3;
+      uint32_t part = 0, *wp = nullptr;
+      if (i < total) {
+        const uint32_t inp = i / p.gpad, g = i % p.gpad;
+        const uint32_t reg = __ldg(p.stimReg + inp);
+        const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
+        const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
+        wp = p.regs + size_t(reg) * p.gpad + g;
+        const uint32_t cur = nib(__ldcg(wp), k);
+        uint32_t v = cur;
+        stimValue(p, g * SPW + k, cycle, inp, cur, mask, tog, v);
+        part = v << (4u * k);
+      }
+      part |= __shfl_xor_sync(kFull, part, 1);
+      part |= __shfl_xor_sync(kFull, part, 2);
+      part |= __shfl_xor_sync(kFull, part, 4);
+      if (wp && k == 0) *wp = part;
+    }
+    return;
+  }
   for (uint32_t i = gtid; i < total; i += gthreads) {
     const uint32_t inp = i / p.gpad, g = i % p.gpad;
     const uint32_t reg = __ldg(p.stimReg + inp);
