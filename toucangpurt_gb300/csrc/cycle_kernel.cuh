@@ -851,24 +851,19 @@ __device__ void applyStimulus(const KParams &p, uint32_t cycle, uint32_t gtid, u
       part |= __shfl_xor_sync(kFull, part, 4);
       if (wp && k == 0) *wp = part;
     }
-    return;
-  }
-  for (uint32_t i = gtid; i < total; i += gthreads) {
-    const uint32_t inp = i / p.gpad, g = i % p.gpad;
-    const uint32_t reg = __ldg(p.stimReg + inp);
-    const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
-    const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
-    uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
-    const uint32_t w = __ldcg(wp);
-    uint32_t nw = 0;
-#pragma unroll
-    for (int k = 0; k < SPW; ++k) {
-      const uint32_t cur = nib(w, k);
+  } else {
+    // one stream per word
+    for (uint32_t i = gtid; i < total; i += gthreads) {
+      const uint32_t inp = i / p.gpad, g = i % p.gpad;
+      const uint32_t reg = __ldg(p.stimReg + inp);
+      const uint32_t mask = (1u << __ldg(p.stimBits + inp)) - 1u;
+      const uint32_t tog = p.stimToggle ? uint32_t(__ldg(p.stimToggle + inp)) : 0u;
+      uint32_t *wp = p.regs + size_t(reg) * p.gpad + g;
+      const uint32_t cur = nib(__ldcg(wp), 0);
       uint32_t v = cur;
-      stimValue(p, g * SPW + k, cycle, inp, cur, mask, tog, v);
-      nw |= v << (4 * k);
+      stimValue(p, g, cycle, inp, cur, mask, tog, v);
+      *wp = v;
     }
-    *wp = nw;
   }
 }
 
