@@ -112,7 +112,9 @@ class OracleDesign:
             return np.zeros(0, np.uint8)
         return np.ctypeslib.as_array(lib().orc_initial_mems(self._d), (self.mem_pool,)).copy()
 
-    def run(self, cycles, stim=None, *, threads=0, cycle_digests=False, final_state=False):
+    def run(self, cycles, stim=None, *, threads=0, cycle_digests=False, final_state=False, final_digests=True):
+        """final_digests=False skips the final register and memory digests
+        (the memory digest reads every stream's whole pool)."""
         cyc = np.ascontiguousarray(cycles, np.uint32)
         n = cyc.size
         out = {k: np.zeros(n, np.uint64) for k in ("final_reg_digest", "final_mem_digest", "rolling_digest")}
@@ -123,7 +125,8 @@ class OracleDesign:
         if final_state:
             out["final_regs"] = np.zeros((n, self.reg_pool), np.uint8)
             out["final_mems"] = np.zeros((n, max(1, self.mem_pool)), np.uint8)
-        res = Result(_p(out["final_reg_digest"], C.c_uint64), _p(out["final_mem_digest"], C.c_uint64),
+        fin = (lambda a: _p(a, C.c_uint64)) if final_digests else (lambda a: _p(None, C.c_uint64))
+        res = Result(fin(out["final_reg_digest"]), fin(out["final_mem_digest"]),
                      _p(out["rolling_digest"], C.c_uint64), _p(out.get("cycle_digest"), C.c_uint64), stride,
                      _p(out["stop_cycle"], C.c_uint32), _p(out.get("final_regs"), C.c_uint8),
                      _p(out.get("final_mems"), C.c_uint8))
