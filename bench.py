@@ -56,8 +56,10 @@ def args_parse():
     p.add_argument("--value-pool", default="compact", choices=["compact", "design"],
                    help="value-pool slots renumbered by live range (default) or as numbered in the design file")
     p.add_argument("--autotune", action="store_true", help="time the launch configurations first and keep the fastest")
-    p.add_argument("--mode", default="graph", choices=["persistent", "graph"],
-                   help="cycle loop as one persistent launch or as replayed CUDA-graph chunks (one launch per region)")
+    p.add_argument("--mode", default="auto", choices=["auto", "persistent", "graph"],
+                   help="cycle loop as one persistent launch or as replayed CUDA-graph chunks (one launch per region); "
+                        "auto: persistent when the exec levels stay resident in shared memory (short, latency-bound "
+                        "levels: one launch keeps them for the whole run), else graph")
     p.add_argument("--slots", type=int, default=0, help="resident slots for queued streams of uneven length")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cycles", type=int, default=5)
@@ -308,9 +310,12 @@ def exec_levels(st) -> str:
 
 
 def prepare(a, s):
-    """Learned schedule (profile micro-partitions, train the cost model) and
-    autotuning, both before the timed region.  Returns notes for `config`."""
+    """Mode choice (--mode auto), learned schedule (profile micro-partitions,
+    train the cost model) and autotuning, all before the timed region.
+    Returns notes for `config`."""
     notes = {}
+    if a.mode == "auto" and s.design_stats().get("resident_words"):
+        s.set_options(mode=0)  # persistent: resident levels are loaded once per run
     if a.schedule == "learned":
         rep = s.train_cost_model(s.mpart_features(), s.profile_mparts(20), epochs=40, seed=5)
         s.set_options(schedule=1)
@@ -329,7 +334,7 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     from toucangpurt_gb300 import sim, workloads
 
     s = sim.Simulator(n_streams=a.slots or 8, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=levels_option(a), mode=1 if a.mode == "graph" else 0,
+                      resident_netlist=levels_option(a), mode=1 if a.mode != "persistent" else 0,
                       value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
@@ -359,6 +364,7 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams of log-uniform length "
                                    f"(mean {cyc.mean():.0f}), {s.options()['n_streams']} slots, longest first",
                        "stream_cycles": int(cyc.sum()), "schedule": a.schedule, "exec_levels": exec_levels(st),
+                       "mode": ["persistent", "graph"][s.options()["mode"]],
                        "blocks": st["blocks"],
                        "threads_per_block": st["threads"],
                        "groups_per_item": st["groups_per_item"], **notes},
@@ -420,7 +426,7 @@ def run_gb300(a, rank, ws):
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
         return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
     s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=levels_option(a), mode=1 if a.mode == "graph" else 0,
+                      resident_netlist=levels_option(a), mode=1 if a.mode != "persistent" else 0,
                       value_pool=0 if a.value_pool == "compact" else 1)
     s.init(gpu, dp, sp, False, False)
     notes = prepare(a, s)
