@@ -67,9 +67,14 @@ __device__ __forceinline__ void raiseErr(const KParams &p, uint32_t code, uint32
 // an exec level that is staged or not, would otherwise compile to generic
 // accesses with 64-bit address arithmetic.)  Stores carry a memory clobber;
 // loads are volatile, so the compiler keeps them in order with the stores.
-__device__ __forceinline__ uint32_t ldsU8(uint32_t a) {
+// Truth-table reads are the exception: the table is written once, before the
+// block barrier that ends the block's set-up, and never again, so its loads
+// are plain (not volatile) and the compiler may schedule them freely among
+// the value-pool accesses (their addresses depend on operands read after
+// the set-up, which keeps them after it).
+__device__ __forceinline__ uint32_t ldsTab(uint32_t a) {
   uint32_t v;
-  asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
+  asm("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
   return v;
 }
 __device__ __forceinline__ uint32_t ldsU32(uint32_t a) {
@@ -129,7 +134,7 @@ __device__ __forceinline__ uint32_t lookup(uint32_t tab, uint32_t base, uint32_t
 
 template <>
 __device__ __forceinline__ uint32_t lookup<1>(uint32_t tab, uint32_t base, uint32_t A, uint32_t B, uint32_t C) {
-  return ldsU8(tab + base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
+  return ldsTab(tab + base + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
 }
 
 // prmt.b32 in its generic mode: a selector nibble with bit 3 set fills the
@@ -154,10 +159,10 @@ __device__ __forceinline__ uint32_t lookup<8>(uint32_t tab, uint32_t base, uint3
   const uint32_t bcO = (B & 0xF0F0F0F0u) | ((C >> 4) & 0x0F0F0F0Fu);
   const uint32_t aE = A & 0x0F0F0F0Fu, aO = (A >> 4) & 0x0F0F0F0Fu;
   // selector for byte j: result bytes (bc.j, a.j, sign(a.j), sign(a.j))
-  const uint32_t r0 = ldsU8(t + prmtIdx(bcE, aE, 0xCC40u)), r2 = ldsU8(t + prmtIdx(bcE, aE, 0xDD51u));
-  const uint32_t r4 = ldsU8(t + prmtIdx(bcE, aE, 0xEE62u)), r6 = ldsU8(t + prmtIdx(bcE, aE, 0xFF73u));
-  const uint32_t r1 = ldsU8(t + prmtIdx(bcO, aO, 0xCC40u)), r3 = ldsU8(t + prmtIdx(bcO, aO, 0xDD51u));
-  const uint32_t r5 = ldsU8(t + prmtIdx(bcO, aO, 0xEE62u)), r7 = ldsU8(t + prmtIdx(bcO, aO, 0xFF73u));
+  const uint32_t r0 = ldsTab(t + prmtIdx(bcE, aE, 0xCC40u)), r2 = ldsTab(t + prmtIdx(bcE, aE, 0xDD51u));
+  const uint32_t r4 = ldsTab(t + prmtIdx(bcE, aE, 0xEE62u)), r6 = ldsTab(t + prmtIdx(bcE, aE, 0xFF73u));
+  const uint32_t r1 = ldsTab(t + prmtIdx(bcO, aO, 0xCC40u)), r3 = ldsTab(t + prmtIdx(bcO, aO, 0xDD51u));
+  const uint32_t r5 = ldsTab(t + prmtIdx(bcO, aO, 0xEE62u)), r7 = ldsTab(t + prmtIdx(bcO, aO, 0xFF73u));
   const uint32_t lo = __byte_perm(__byte_perm(r0, r2, 0x0040), __byte_perm(r4, r6, 0x0040), 0x5410);
   const uint32_t hi = __byte_perm(__byte_perm(r1, r3, 0x0040), __byte_perm(r5, r7, 0x0040), 0x5410);
   return lo | (hi << 4);
