@@ -276,8 +276,12 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
   }
   // middle levels: operand < 32 immediate, 32..63 = lane (op - 32) of the previous level
   const Words<SH> mid = top.at(2u * W);
+  // each level's op word is read one level ahead, so its latency overlaps
+  // the previous level's shuffles and lookups
+  uint32_t wNext = nMid && lane < W ? mid[lane] : 0u;
   for (uint32_t m = 0; m < nMid; ++m) {
-    const uint32_t w = lane < W ? mid[m * W + lane] : 0u;
+    const uint32_t w = wNext;
+    wNext = m + 1 < nMid && lane < W ? mid[(m + 1) * W + lane] : 0u;
     const uint32_t c6 = w & 63u, b6 = (w >> 6) & 63u, a6 = (w >> 12) & 63u, lut = w >> 18;
     uint32_t nv[H];
 #pragma unroll
