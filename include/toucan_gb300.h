@@ -75,7 +75,10 @@ typedef struct tgs_options {
                                 Takes effect at the next tgs_init / tgs_init_from_memory */
   uint32_t capture_signals;  /* 1: record every signal of the symbol file each cycle (tgs_read_signal, VCD);
                                 takes effect at the next tgs_init (tgs_enable_vcd also turns it on) */
-  uint32_t reserved[5];
+  uint32_t lane_packing;     /* 0 (default): LUT micro-partitions of up to 16 lanes in one exec level are laid side
+                                by side into 32-lane ones (same values, fewer warp passes); 1: the design file's
+                                micro-partitions as they are.  Takes effect at the next tgs_init */
+  uint32_t reserved[4];
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u
@@ -401,6 +404,16 @@ int tgs_validate_file(const char *design_path, const char *symbol_path, uint64_t
  * value_pool option is 0 (no counterpart in the reference).  max_before /
  * max_after (optional): the largest valuePoolSize before and after. */
 int tgs_compact_design(const char *in_path, const char *out_path, uint32_t *max_before, uint32_t *max_after);
+/* Writes the design with the lane packing tgs_init applies by default
+ * (options.lane_packing = 0): in every exec level, LUT micro-partitions of up
+ * to 16 lanes laid side by side into 32-lane ones, each member's lane
+ * references shifted to its lanes and shallower members carried through the
+ * extra middle levels by moves of their own lanes.  The result is a valid
+ * design of the same format that computes the same values (so any evaluator,
+ * the CPU oracle included, can check the packing).  No counterpart in the
+ * reference.  mparts_before / mparts_after: micro-partitions in all exec
+ * levels (either may be NULL). */
+int tgs_pack_design(const char *in_path, const char *out_path, uint32_t *mparts_before, uint32_t *mparts_after);
 
 #ifdef __cplusplus
 }

@@ -39,7 +39,8 @@ class Options(C.Structure):
         ("n_streams", C.c_uint32), ("warps_per_block", C.c_uint32), ("groups_per_item", C.c_uint32),
         ("blocks_per_sm", C.c_uint32), ("schedule", C.c_uint32), ("mode", C.c_uint32),
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
-        ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("reserved", C.c_uint32 * 5),
+        ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("lane_packing", C.c_uint32),
+        ("reserved", C.c_uint32 * 4),
     ]
 
 
@@ -173,6 +174,7 @@ SIGNATURES = {
     "tgs_gen_inputs": [C.POINTER(GenConfig), u32p, u8p, C.c_uint32],
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
     "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
+    "tgs_pack_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_dump_state": [C.c_void_p, C.c_char_p],
     "tgs_read_signal_stream": [C.c_void_p, C.c_uint32, C.c_char_p, C.POINTER(C.c_uint64)],
     "tgs_enable_vcd": [C.c_void_p, C.c_char_p],

@@ -79,6 +79,115 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
   return off;
 }
 
+// ---- lane packing of narrow LUT micro-partitions --------------------------
+// A LUT micro-partition of W lanes occupies a whole warp for its top level,
+// its middle levels and its write-back.  Narrow ones (W <= kPackMaxLanes) of
+// one exec level are laid side by side into 32-lane micro-partitions: member
+// k keeps its ops on lanes [off_k, off_k + W_k), its lane references (middle
+// operands 32..63, write-back shuffle ids >= 32) move by off_k, a member with
+// fewer middle levels carries its values through the extra levels with
+// moves of its own lane (lut 0 passes op2, SimEval.cu:350-352), and idle
+// lanes keep the zero ops that give them the value 0 as before.  Members
+// touch disjoint value-pool slots (micro-partitions of one level do), so the
+// packed one computes exactly what the members did.  A member qualifies only
+// if every lane it references lies inside its own W lanes.
+constexpr uint32_t kPackMaxLanes = 16;
+
+uint32_t lutWidth(const CGMicroPartInfo &m) {
+  uint32_t W = uint32_t(m.topLevel.size());
+  for (auto &l : m.middleLevels) W = std::max<uint32_t>(W, uint32_t(l.size()));
+  return std::max<uint32_t>(std::max<uint32_t>(W, uint32_t(m.lastLevel.size())), 1);
+}
+
+bool packable(const CGMicroPartInfo &m) {
+  if (!m.isLUTPart || m.lastLevel.empty()) return false;
+  const uint32_t W = lutWidth(m);
+  if (W > kPackMaxLanes) return false;
+  for (auto &lvl : m.middleLevels)
+    for (auto &op : lvl)
+      for (uint32_t x : {uint32_t(op.op0()), uint32_t(op.op1()), uint32_t(op.op2())})
+        if (x >= 32 && x - 32 >= W) return false;
+  for (auto &w : m.lastLevel)
+    if (w.shuffleId >= 32 && (w.shuffleId & 31u) >= W) return false;
+  return true;
+}
+
+CGMicroPartInfo packMembers(const std::vector<CGMicroPartInfo> &in, const std::vector<uint32_t> &members) {
+  CGMicroPartInfo out;
+  out.isLUTPart = true;
+  uint32_t nMid = 0, lanes = 0;
+  for (uint32_t i : members) {
+    nMid = std::max<uint32_t>(nMid, uint32_t(in[i].middleLevels.size()));
+    lanes += lutWidth(in[i]);
+  }
+  out.topLevel.assign(lanes, CGMicroPartLUTTopLevelOp{0, 0, 0, 0});
+  out.middleLevels.assign(nMid, std::vector<CGMicroPartLUTMiddleLevelOp>(lanes));
+  auto lane = [](uint32_t x, uint32_t off) { return uint8_t(x >= 32 ? 32 + off + (x & 31u) : x); };
+  uint32_t off = 0;
+  for (size_t k = 0; k < members.size(); ++k) {
+    const CGMicroPartInfo &m = in[members[k]];
+    const uint32_t W = lutWidth(m);
+    for (size_t l = 0; l < m.topLevel.size(); ++l) out.topLevel[off + l] = m.topLevel[l];
+    for (uint32_t lv = 0; lv < nMid; ++lv)
+      for (uint32_t l = 0; l < W; ++l) {
+        auto &dst = out.middleLevels[lv][off + l];
+        if (lv < m.middleLevels.size()) {
+          if (l < m.middleLevels[lv].size()) {
+            const auto &op = m.middleLevels[lv][l];
+            dst = CGMicroPartLUTMiddleLevelOp(op.lutIndex(), lane(op.op0(), off), lane(op.op1(), off), lane(op.op2(), off));
+          }  // else a zero op, as the member's idle lane had
+        } else {
+          dst = CGMicroPartLUTMiddleLevelOp(0, 0, 0, uint8_t(32 + off + l));  // carry the lane's value
+        }
+      }
+    // write-back entry l sits on lane l: the member's entries on its lanes;
+    // lanes between its entries and the next member repeat its last entry
+    // (the same value into the same slot)
+    const uint32_t nWB = uint32_t(m.lastLevel.size());
+    const bool last = k + 1 == members.size();
+    for (uint32_t l = 0; l < (last ? nWB : W); ++l) {
+      CGMicroPartLUTLastLevelWriteBack w = m.lastLevel[std::min(l, nWB - 1)];
+      w.shuffleId = lane(w.shuffleId >= 64 ? 32u + (w.shuffleId & 31u) : w.shuffleId, off);
+      out.lastLevel.push_back(w);
+    }
+    off += W;
+  }
+  return out;
+}
+
+}  // namespace
+
+// The exec level with its narrow LUT micro-partitions packed (first fit,
+// deepest and widest first, so members of a packed one have similar depth).
+std::vector<CGMicroPartInfo> packLevel(const std::vector<CGMicroPartInfo> &in) {
+  std::vector<uint32_t> cand, out;
+  std::vector<CGMicroPartInfo> res;
+  for (uint32_t i = 0; i < in.size(); ++i) (packable(in[i]) ? cand : out).push_back(i);
+  if (cand.size() < 2) return in;
+  std::stable_sort(cand.begin(), cand.end(), [&](uint32_t a, uint32_t b) {
+    const size_t da = in[a].middleLevels.size(), db = in[b].middleLevels.size();
+    return da != db ? da > db : lutWidth(in[a]) > lutWidth(in[b]);
+  });
+  std::vector<std::vector<uint32_t>> bins;
+  std::vector<uint32_t> used;
+  for (uint32_t i : cand) {
+    const uint32_t W = lutWidth(in[i]);
+    size_t b = 0;
+    while (b < bins.size() && used[b] + W > 32) ++b;
+    if (b == bins.size()) {
+      bins.emplace_back();
+      used.push_back(0);
+    }
+    bins[b].push_back(i);
+    used[b] += W;
+  }
+  for (uint32_t i : out) res.push_back(in[i]);
+  for (auto &b : bins) res.push_back(b.size() == 1 ? in[b[0]] : packMembers(in, b));
+  return res;
+}
+
+namespace {
+
 uint32_t emitSpecial(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f) {
   align4(net);
   uint32_t off = uint32_t(net.size());
@@ -172,7 +281,7 @@ void accessOf(const CGMicroPartInfo &m, std::vector<uint32_t> &rd, std::vector<u
 
 }  // namespace
 
-void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, const ProbeList *probes) {
+void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, const ProbeList *probes, bool packLanes) {
   img = DeviceImage();
   img.parts.resize(d.parts.size());
   img.mp.resize(d.parts.size());
@@ -222,7 +331,9 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, con
     pd.nLevels = uint32_t(p.exec_mParts.size());
     img.mp[pid].resize(pd.nLevels);
     for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
-      for (const auto &m : p.exec_mParts[lv]) {
+      std::vector<CGMicroPartInfo> packed;
+      if (packLanes) packed = packLevel(p.exec_mParts[lv]);
+      for (const auto &m : packLanes ? packed : p.exec_mParts[lv]) {
         MPartRef ref;
         ref.feat.partLevels = pd.nLevels;
         ref.off = m.isLUTPart ? emitLut(m, net, ref.feat) : emitSpecial(m, net, ref.feat);

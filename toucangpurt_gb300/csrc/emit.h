@@ -65,8 +65,13 @@ struct Schedule {
 // probes (optional): per partition, (value-pool slot, probe index) pairs
 // whose values the kernel records after the exec levels (signal capture).
 using ProbeList = std::vector<std::vector<std::pair<uint32_t, uint32_t>>>;
+// One exec level with its LUT micro-partitions of up to 16 lanes laid side by
+// side into 32-lane ones (same values; emit.cpp).
+std::vector<toucanGPUSim::CGMicroPartInfo> packLevel(const std::vector<toucanGPUSim::CGMicroPartInfo> &in);
+
+// packLanes: packLevel applied to every exec level.
 void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots,
-                const ProbeList *probes = nullptr);
+                const ProbeList *probes = nullptr, bool packLanes = false);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
 // G: stream groups per item (special micro-partitions are split by group).
 void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,

@@ -495,7 +495,8 @@ void buildProbes(tgs_sim *h) {
 void upload(tgs_sim *h) {
   cudaStream_t s = h->stream;
   buildProbes(h);
-  buildImage(h->design, h->img, h->opt.value_pool == 0, h->captureSignals ? &h->probes : nullptr);
+  buildImage(h->design, h->img, h->opt.value_pool == 0, h->captureSignals ? &h->probes : nullptr,
+             h->opt.lane_packing == 0);
   h->net.upload(h->img.net, s);
   h->constVec.upload(h->img.constVec, s);
   std::vector<uint8_t> lut(kLutTablePadded, 0);
@@ -1815,6 +1816,27 @@ extern "C" int tgs_compact_design(const char *in, const char *out, uint32_t *max
     }
     if (maxBefore) *maxBefore = before;
     if (maxAfter) *maxAfter = after;
+    std::ofstream o(out, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
+    serializeSimDesignInfo(o, d);
+  });
+}
+
+extern "C" int tgs_pack_design(const char *in, const char *out, uint32_t *mparts_before, uint32_t *mparts_after) {
+  return guard([&] {
+    if (!in || !out) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(in);
+    SimDesignInfo d;
+    parseDesign(bytes.data(), bytes.size(), d);
+    uint32_t before = 0, after = 0;
+    for (auto &p : d.parts)
+      for (auto &lvl : p.exec_mParts) {
+        before += uint32_t(lvl.size());
+        lvl = packLevel(lvl);
+        after += uint32_t(lvl.size());
+      }
+    if (mparts_before) *mparts_before = before;
+    if (mparts_after) *mparts_after = after;
     std::ofstream o(out, std::ios::binary);
     if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
     serializeSimDesignInfo(o, d);
