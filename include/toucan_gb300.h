@@ -59,7 +59,7 @@ int tgs_destroy(tgs_sim *h);
 /* ---- tuning ----------------------------------------------------------- */
 typedef struct tgs_options {
   uint32_t n_streams;        /* independent design copies (default 1) */
-  uint32_t warps_per_block;  /* 1 to 32; 0 = the most common exec-level width of the design (4..16) */
+  uint32_t warps_per_block;  /* 1 to 32; 0 = the most common exec-level width of the design (6..16) */
   uint32_t groups_per_item;  /* 8-stream groups one block evaluates together: 1, 2, 4 or 8; 0 = 4, halved
                                 while a region would have fewer than two items per SM */
   uint32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid (0 = max) */
