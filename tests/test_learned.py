@@ -89,14 +89,18 @@ def test_training_learns_costs_and_keeps_values_exact(mixed_design):
 
 
 @pytest.mark.gpu
-def test_learned_schedule_gain(mixed_design):
+@pytest.mark.parametrize("packing", [0, 1])
+def test_learned_schedule_gain(mixed_design, packing):
     """Measured cycle time of the learned schedule against the gate-count one
-    on the heterogeneous design (same streams, same cycles)."""
+    on the heterogeneous design (same streams, same cycles), with the narrow
+    control cones packed into full warps (the default) and as the design
+    file has them (one warp pass per 4-8-lane cone, where gate count is the
+    poorest guide to cost)."""
     dp, sp, info = mixed_design
     n, cycles = 64, 60
     stim = sim.StimulusSpec(8, info["pi_ids"], info["pi_bits"])
     cyc = np.full(n, cycles, np.uint32)
-    with sim.Simulator(n_streams=n) as s:
+    with sim.Simulator(n_streams=n, lane_packing=packing) as s:
         s.init(0, dp, sp, False, False)
         s.train_cost_model(s.mpart_features(), s.profile_mparts(20), epochs=40, seed=5)
         t = {}
@@ -104,5 +108,6 @@ def test_learned_schedule_gain(mixed_design):
             s.set_options(schedule=sched)
             s.batch_run(cyc, stim, rolling=False)  # warm
             t[name] = min(s.batch_run(cyc, stim, rolling=False).device_ms for _ in range(3))
-    print(f"greedy {t['greedy']:.2f} ms, learned {t['learned']:.2f} ms, gain {t['greedy'] / t['learned']:.3f}x")
+    print(f"lane_packing={packing}: greedy {t['greedy']:.2f} ms, learned {t['learned']:.2f} ms, "
+          f"gain {t['greedy'] / t['learned']:.3f}x")
     assert t["learned"] <= t["greedy"] * 1.05
