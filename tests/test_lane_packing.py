@@ -64,6 +64,7 @@ def test_packed_design_evaluates_like_original(narrow, tmp_path, name):
     dst = tmp_path / "p.bin"
     before, after = pack(dp, dst)
     assert after < before  # something was packed
+    capi.check(capi.lib().tgs_validate_file(str(dst).encode(), str(sp).encode(), None))  # still a valid design
     cycles = np.full(3, 40, np.uint32)
     stim = sim.StimulusSpec(31, info["pi_ids"], info["pi_bits"])
     a = pyoracle.OracleDesign(dp, sp).run(cycles, stim, cycle_digests=True)
