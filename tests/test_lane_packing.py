@@ -88,3 +88,59 @@ def test_gpu_packing_matches_oracle(narrow, name, packing, mode):
     for k in ("final_reg_digest", "final_mem_digest", "rolling_digest", "stop_cycle"):
         np.testing.assert_array_equal(getattr(got, k), ref[k], err_msg=k)
     np.testing.assert_array_equal(got.cycle_digest, ref["cycle_digest"])
+
+
+def _packing_kat():
+    """One exec level of four narrow micro-partitions: A references a lane
+    beyond its width (not packable: that lane is idle, value 0, in A alone);
+    B has two middle levels, an immediate write-back and a shuffle id >= 64;
+    C has fewer write-back entries than lanes; D has one middle level."""
+    from tests import designlib as dl
+    from tests.test_kat import IN, OUT, frame, table
+
+    lut = table(100, lambda a, b, c: a * 7 + b * 3 + c * 5 + (a & b), rows=16)
+    A = dl.MPart(top=[dl.top(100, IN + 0, IN + 1, IN + 2), dl.top(100, IN + 3, IN + 4, IN + 5),
+                      dl.top(100, 1, IN + 6, IN + 7)],
+                 mids=[[dl.mid(100, 33, 34, 37), dl.mid(100, 32, 32, 33), dl.mid(0, 0, 0, 34)]],
+                 wbs=[dl.wb(32, OUT + 0), dl.wb(33, OUT + 1), dl.wb(34, OUT + 2)])
+    B = dl.MPart(top=[dl.top(100, IN + 8, IN + 9, IN + 10), dl.top(100, 2, IN + 11, IN + 12),
+                      dl.top(100, IN + 13, 4, IN + 14), dl.top(0, 0, 0, IN + 15)],
+                 mids=[[dl.mid(100, 33, 34, 35), dl.mid(100, 32, 35, 34), dl.mid(100, 34, 33, 32), dl.mid(0, 0, 0, 35)],
+                       [dl.mid(100, 32, 33, 34), dl.mid(100, 35, 34, 33), dl.mid(0, 0, 0, 33), dl.mid(100, 3, 32, 35)]],
+                 wbs=[dl.wb(32, OUT + 3), dl.wb(7, OUT + 4), dl.wb(64 + 2, OUT + 5), dl.wb(35, OUT + 6)])
+    C = dl.MPart(top=[dl.top(100, IN + 1, IN + 3, IN + 5), dl.top(100, IN + 2, IN + 4, IN + 6)],
+                 wbs=[dl.wb(33, OUT + 7)])
+    D = dl.MPart(top=[dl.top(100, IN + k, IN + (k + 5) % 16, IN + (k + 9) % 16) for k in range(5)],
+                 mids=[[dl.mid(100, 32 + (k + 1) % 5, 32 + k, 32 + (k + 3) % 5) for k in range(5)]],
+                 wbs=[dl.wb(32 + k, OUT + 8 + k) for k in range(5)])
+    return frame([[A, B, C, D]], lut=lut)
+
+
+def test_packing_known_answer_design(tmp_path, built):
+    dp = tmp_path / "kat.bin"
+    _packing_kat().write(dp)
+    dst = tmp_path / "packed.bin"
+    before, after = pack(dp, dst)
+    assert (before, after) == (5, 3)  # B, C and D packed into one; A and the zeroing level kept
+    capi.check(capi.lib().tgs_validate_file(str(dst).encode(), None, None))
+    stim = sim.StimulusSpec(5, np.arange(16, dtype=np.uint32), np.full(16, 4, np.uint8))
+    cycles = np.full(2, 50, np.uint32)
+    a = pyoracle.OracleDesign(dp).run(cycles, stim, cycle_digests=True, final_state=True)
+    b = pyoracle.OracleDesign(dst).run(cycles, stim, cycle_digests=True, final_state=True)
+    for k in ("cycle_digest", "final_regs", "final_mems", "stop_cycle"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("packing", [0, 1])
+def test_packing_known_answer_design_gpu(tmp_path, built, packing):
+    dp = tmp_path / "kat.bin"
+    _packing_kat().write(dp)
+    stim = sim.StimulusSpec(5, np.arange(16, dtype=np.uint32), np.full(16, 4, np.uint8))
+    cycles = np.full(16, 50, np.uint32)
+    ref = pyoracle.OracleDesign(dp).run(cycles, stim, cycle_digests=True)
+    with sim.Simulator(n_streams=16, lane_packing=packing) as s:
+        s.init(0, dp, None, False, False)
+        got = s.batch_run(cycles, stim, cycle_digests=True)
+    np.testing.assert_array_equal(got.cycle_digest, ref["cycle_digest"])
+    np.testing.assert_array_equal(got.final_reg_digest, ref["final_reg_digest"])
