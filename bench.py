@@ -61,9 +61,14 @@ def args_parse():
                         "auto: persistent when the exec levels stay resident in shared memory (short, latency-bound "
                         "levels: one launch keeps them for the whole run), else graph")
     p.add_argument("--slots", type=int, default=0, help="resident slots for queued streams of uneven length")
-    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline and the oracle parity check")
+    p.add_argument("--no-baselines", action="store_true",
+                   help="skip the plain single-stream form and the reference kernel run after the timed region")
+    p.add_argument("--ref-cycles", type=int, default=20, help="cycles of the reference kernel's eval() run")
     p.add_argument("--cpu-sample-cycles", type=int, default=5)
     p.add_argument("--out", default="")
+    p.add_argument("--set", action="append", default=[], metavar="OPTION=VALUE",
+                   help="further tgs_options field of the simulator (e.g. fast_luts=1 for table lookups only)")
     p.add_argument("--override", action="append", default=[],
                    help="generator field override key=value (e.g. a smaller memory depth for profiling)")
     return p.parse_args()
@@ -215,17 +220,6 @@ def cpu_cycles_time(od, stim, streams, cycles, threads):
     return max((t2 - t1) - (t1 - t0), 1e-9)
 
 
-def cpu_baseline(dp, sp, info, workload, streams, cycles, threads):
-    """Oracle port on the host cores, bounded sample of the same workload."""
-    from oracle import pyoracle
-    from toucangpurt_gb300 import sim, workloads
-
-    od = pyoracle.OracleDesign(dp, sp)
-    stim = sim.StimulusSpec(1234, info["pi_ids"], info["pi_bits"], workloads.toggles(workload, info["pi_bits"]))
-    dt = cpu_cycles_time(od, stim, streams, cycles, threads)
-    return streams * cycles / dt, dt
-
-
 def run_reference(a, rank, ws):
     """Reference arm: CPU evaluation of the workload on all host threads."""
     if rank != 0:
@@ -309,22 +303,23 @@ def exec_levels(st) -> str:
     return "resident" if st.get("resident_words") else "staged" if st.get("stage_words") else "global"
 
 
-def prepare(a, s):
-    """Mode choice (--mode auto), learned schedule (profile micro-partitions,
-    train the cost model) and autotuning, all before the timed region.
-    Returns notes for `config`."""
-    notes = {}
-    if a.mode == "auto" and s.design_stats().get("resident_words"):
-        s.set_options(mode=0)  # persistent: resident levels are loaded once per run
-    if a.schedule == "learned":
-        rep = s.train_cost_model(s.mpart_features(), s.profile_mparts(20), epochs=40, seed=5)
-        s.set_options(schedule=1)
-        notes["cost_model"] = {k: round(float(v), 4) for k, v in rep.items() if k in ("val_mse", "val_corr", "gate_corr")}
+def make_simulator(a, dp, sp, streams, gpu):
+    """The simulator configured as the benchmark runs the workload
+    (workloads.bench_simulator: mode choice, learned schedule trained before
+    the timed region), then autotuned when asked.  Returns (sim, notes)."""
+    from toucangpurt_gb300 import workloads
+
+    s, notes = workloads.bench_simulator(a.workload, dp, sp, streams=streams, gpu=gpu, schedule=a.schedule,
+                                         mode=a.mode, groups=a.groups, warps=a.warps, levels=levels_option(a),
+                                         value_pool=0 if a.value_pool == "compact" else 1,
+                                         **{k: int(v) for k, v in (kv.split("=", 1) for kv in a.set)})
+    if a.set:
+        notes["options"] = list(a.set)
     if a.autotune:
         best, trials = s.autotune(cycles=8, warmup=2)
         notes["autotuned"] = {k: best[k] for k in ("groups_per_item", "warps_per_block", "blocks_per_sm", "mode", "staged")}
         notes["autotune_trials"] = len(trials)
-    return notes
+    return s, notes
 
 
 def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
@@ -333,11 +328,7 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
     graph replays).  One step = the whole job."""
     from toucangpurt_gb300 import sim, workloads
 
-    s = sim.Simulator(n_streams=a.slots or 8, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=levels_option(a), mode=1 if a.mode != "persistent" else 0,
-                      value_pool=0 if a.value_pool == "compact" else 1)
-    s.init(gpu, dp, sp, False, False)
-    notes = prepare(a, s)
+    s, notes = make_simulator(a, dp, sp, a.slots or 8, gpu)
     cyc = workloads.stream_lengths(a.workload, streams, seed=7 + rank)
     stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], workloads.toggles(a.workload, info["pi_bits"]))
     for _ in range(a.warmup):
@@ -411,6 +402,70 @@ def run_e2e(a, s, info, stim, streams, cps):
     return dt, int(cps * n_in * streams), int(streams * (8 + 4))
 
 
+def parity_check(od, s, stim, timed, streams, cps, cycles, threads):
+    """The oracle against this library on the benchmark's own inputs: the
+    per-cycle register digests of every stream over the first `cycles`
+    cycles of a timed step, and the final register, memory and rolling
+    digests of a separate `cycles`-cycle run (memories included)."""
+    c = max(1, min(cycles, cps))
+    ref = od.run(np.full(streams, c, np.uint32), stim, threads=threads, cycle_digests=True)
+    short = s.batch_run(np.full(streams, c, np.uint32), stim)
+    bad = []
+    if not np.array_equal(timed.cycle_digest[:, :c], ref["cycle_digest"]):
+        bad.append("per-cycle register digests")
+    for k in ("final_reg_digest", "final_mem_digest", "rolling_digest", "stop_cycle"):
+        if not np.array_equal(getattr(short, k), ref[k]):
+            bad.append(k)
+    return {"result": "bit-exact" if not bad else "MISMATCH: " + ", ".join(bad), "against": "CPU oracle",
+            "checked": f"{streams} streams x {c} cycles: per-cycle register digests of a timed step; final register, "
+                       f"memory and rolling digests and stop cycles of a {c}-cycle run"}
+
+
+def plain_form(a, dp, sp, info, gpu, cps, stim):
+    """The plain form on the same design: one stream, gate-count schedule,
+    the same cycles per step; device time per step (CUDA events)."""
+    from toucangpurt_gb300 import workloads
+
+    s, _ = workloads.bench_simulator(a.workload, dp, sp, streams=1, gpu=gpu, schedule="greedy", mode=a.mode,
+                                     **{k: int(v) for k, v in (kv.split("=", 1) for kv in a.set)})
+    cyc = np.full(1, cps, np.uint32)
+    for _ in range(a.warmup):
+        s.batch_run(cyc, stim)
+    ms = sum(s.batch_run(cyc, stim).device_ms for _ in range(a.steps))
+    opts = s.options()
+    s.cleanup()
+    return {"value": cps * a.steps / (ms / 1000.0), "unit": "stimulus-cycles/s", "streams": 1, "schedule": "greedy",
+            "mode": ["persistent", "graph"][opts["mode"]]}
+
+
+def reference_kernel(dp, sp, info, stim, timed, cycles):
+    """The reference's own GPU kernel on the same design: its race-free
+    eval() path (evalSingleCycle, one cooperative launch per cycle with the
+    inputs written between cycles, src/ToucanSim.cu:206-230), one stream,
+    kernel time from CUDA events; its per-cycle register digests are
+    compared with stream 0 of a timed step of this library."""
+    from oracle import pyoracle
+
+    exe, cubin = pyoracle.HERE / "_build" / "refgpu", pyoracle.REF_CUBIN
+    if not exe.exists() or not cubin.exists():
+        return {"unavailable": "reference cubin not built here (built from the reference checkout by oracle/Makefile)"}
+    wd = Path(tempfile.mkdtemp(prefix="tgs_refk_"))
+    tog = stim.toggle if stim.toggle is not None else np.zeros(len(stim.reg), np.uint16)
+    (wd / "stim.txt").write_text(f"{stim.base_seed} {len(stim.reg)}\n" + "".join(
+        f"{int(r)} {int(b)} {int(g)}\n" for r, b, g in zip(stim.reg, stim.bits, tog)))
+    out = wd / "eval.jsonl"
+    t0 = time.perf_counter()
+    subprocess.run([str(exe), str(cubin), str(dp), str(sp), "0", "eval", str(cycles), "1", str(wd / "stim.txt"),
+                    str(out)], check=True, timeout=1800, stdout=subprocess.DEVNULL)
+    r = json.loads(out.read_text().splitlines()[0])
+    digs = np.array([int(x, 16) for x in r["cycle_digests"]], np.uint64)
+    same = bool(np.array_equal(digs, timed.cycle_digest[0, :cycles]))
+    return {"value": cycles / (r["kernel_ms"] / 1e3), "unit": "stimulus-cycles/s", "path": "eval() (evalSingleCycle)",
+            "streams": 1, "cycles": cycles, "threads": r["threads"], "grid": r["grid_single"],
+            "parity": "bit-exact (stream 0, per-cycle register digests)" if same else "MISMATCH",
+            "wall_s": round(time.perf_counter() - t0, 1)}
+
+
 def run_gb300(a, rank, ws):
     from toucangpurt_gb300 import build, sim, workloads
 
@@ -425,23 +480,19 @@ def run_gb300(a, rank, ws):
     schedule = 1 if a.schedule == "learned" else 0
     if isinstance(workloads.RUNS[a.workload]["cycles"], tuple):
         return run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu)
-    s = sim.Simulator(n_streams=streams, groups_per_item=a.groups, warps_per_block=a.warps,
-                      resident_netlist=levels_option(a), mode=1 if a.mode != "persistent" else 0,
-                      value_pool=0 if a.value_pool == "compact" else 1)
-    s.init(gpu, dp, sp, False, False)
-    notes = prepare(a, s)
+    s, notes = make_simulator(a, dp, sp, streams, gpu)
     st = s.design_stats()
     toggle = workloads.toggles(a.workload, info["pi_bits"])
     stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], toggle)
     cyc = np.full(streams, cps, np.uint32)
     for _ in range(a.warmup):
-        s.batch_run(cyc, stim)
+        s.batch_run(cyc, stim, cycle_digests=True)
     barrier(ws)
     clk = Clocks(gpu)
     dev_ms = 0.0
     launches = 0
     for _ in range(a.steps):
-        out = s.batch_run(cyc, stim)
+        out = s.batch_run(cyc, stim, cycle_digests=True)
         dev_ms += out.device_ms
         launches += out.launches
     clocks = clk.stop()
@@ -462,13 +513,25 @@ def run_gb300(a, rank, ws):
     launch_s = dev_ms / 1000.0 / a.steps / launches_step
     achieved = bytes_launch / launch_s / 1e9
     traffic = profiled_traffic() if a.workload == "largest" and streams == 64 else None
-    cpu = None
+    cpu = parity = plain = refk = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        from oracle import pyoracle
+
         nth = cpu_threads(info, streams)
-        cs, cdt = cpu_baseline(dp, sp, info, a.workload, streams, a.cpu_sample_cycles, nth)
-        cpu = {"value": cs, "unit": "stimulus-cycles/s", "cores": nth, "kind": "port",
+        od = pyoracle.OracleDesign(dp, sp)
+        cdt = cpu_cycles_time(od, stim, streams, a.cpu_sample_cycles, nth)
+        cpu = {"value": streams * a.cpu_sample_cycles / cdt, "unit": "stimulus-cycles/s", "cores": nth, "kind": "port",
                "sample": f"{streams} streams x {a.cpu_sample_cycles} cycle(s) of the same design, {cdt:.1f} s "
                          f"(a run of 1 + {a.cpu_sample_cycles} cycles less a run of 1 cycle)"}
+        parity = parity_check(od, s, stim, out, streams, cps, a.cpu_sample_cycles, nth)
+        del od
+    if rank == 0 and ws == 1 and not a.no_baselines:
+        if streams > 1:
+            plain = plain_form(a, dp, sp, info, gpu, cps, stim)
+            plain["batched_over_plain"] = value / plain["value"]
+        refk = reference_kernel(dp, sp, info, stim, out, min(cps, a.ref_cycles))
+        if "value" in refk:
+            refk["batched_over_reference_kernel"] = value / refk["value"]
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "stimulus-cycles/s", "n_gpus": ws, "steps": a.steps,
@@ -476,7 +539,7 @@ def run_gb300(a, rank, ws):
             "vs_baseline": None, "dtype": "u8 nibbles (8 streams per u32)", "data": "synthetic (seeded generator)",
             "config": {"workload": f"{a.workload}: {st['lut_ops']} LUT ops, {streams} streams, {cps} cycles per step",
                        "streams": streams, "cycles_per_step": cps, "lut_ops": st["lut_ops"],
-                       "partitions": st["partitions"], "schedule": a.schedule, "groups_per_item": st["groups_per_item"],
+                       "partitions": st["partitions"], "groups_per_item": st["groups_per_item"],
                        "mode": ["persistent", "graph"][s.options()["mode"]], "value_pool": a.value_pool,
                        "smem_per_block": st.get("smem_per_block"), "exec_levels": exec_levels(st), **notes,
                        "threads_per_block": st["threads"], "blocks": st["blocks"],
@@ -494,6 +557,12 @@ def run_gb300(a, rank, ws):
             "gpu_launches": launches,
             "clocks": clocks,
         }
+        if parity:
+            line["parity"] = parity
+        if plain:
+            line["plain"] = plain
+        if refk:
+            line["reference_kernel"] = refk
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -78,7 +78,12 @@ typedef struct tgs_options {
   uint32_t lane_packing;     /* 0 (default): LUT micro-partitions of up to 16 lanes in one exec level are laid side
                                 by side into 32-lane ones (same values, fewer warp passes); 1: the design file's
                                 micro-partitions as they are.  Takes effect at the next tgs_init */
-  uint32_t reserved[4];
+  uint32_t fast_luts;        /* 0 (default): LUT ops whose table row is a bitwise function of op1 and op2 (AND, OR,
+                                XOR, ...) or a 0/1-select multiplexer -- checked entry by entry against the design's
+                                table at load time -- are computed with word-wide logic for 8 streams at once, and
+                                the ops of single-level LUT micro-partitions of an exec level are regrouped so that
+                                such ops share warps; 1: every op by table lookup.  Takes effect at the next tgs_init */
+  uint32_t reserved[3];
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u
@@ -148,6 +153,11 @@ int tgs_read_register(tgs_sim *h, const char *name, uint64_t *value);
 /* Per-stream variants. */
 int tgs_set_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t value);
 int tgs_read_register_stream(tgs_sim *h, uint32_t stream, const char *name, uint64_t *value);
+/* read_reg_from_gpu for many registers (src/SimEval.cu:1058-1069,
+ * src/ToucanSim.cu:280-289): values[i] = register names[i] of `stream`,
+ * most significant nibble first.  One gather kernel and one device-to-host
+ * copy per call (the reference issues one blocking copy per nibble). */
+int tgs_read_registers(tgs_sim *h, uint32_t stream, const char *const *names, uint32_t n, uint64_t *values);
 
 /* ToucanSimulator::readSignal (src/ToucanSim.cu:291-300; unimplemented in
  * the reference, which returns UINT64_MAX): the value of a signal of the
@@ -211,11 +221,16 @@ int tgs_load_state(tgs_sim *h, const char *path);
  * (bytes < 4 GiB); digests: host array of n_pools results.  At most 4,096
  * pools per call (TGS_ERR_RANGE above that).  Allocates nothing: the
  * per-pool accumulators are a fixed 32 KiB device array inside the library,
- * present on every GPU that loads it until the process exits.  The first
- * call on a device resolves that array's device address (with the device
- * current), so make it before any stream capture.  Runs on the legacy
- * default stream and waits for it; all calls share the one array, so calls
- * that overlap on the GPU (other host threads) race. */
+ * present on every GPU that loads it until the process exits.  Every call
+ * looks up that array's address in the current device's context (so a
+ * context re-created by cudaDeviceReset is followed); the first call on a
+ * device loads the library's device code there, so make it before any
+ * stream capture.  Runs on the legacy default stream and waits for it: the
+ * caller must first synchronise the stream or event that wrote the pools
+ * when that stream does not synchronise with the legacy default stream (a
+ * cudaStreamNonBlocking stream, or code built with per-thread default
+ * streams), else the digests may read stale bytes.  All calls share the
+ * one array, so calls that overlap on the GPU (other host threads) race. */
 int tgs_pool_digests_noalloc(const uint8_t *pools, uint64_t stride, uint64_t bytes, uint32_t n_pools,
                              uint64_t *digests);
 
@@ -414,6 +429,23 @@ int tgs_compact_design(const char *in_path, const char *out_path, uint32_t *max_
  * reference.  mparts_before / mparts_after: micro-partitions in all exec
  * levels (either may be NULL). */
 int tgs_pack_design(const char *in_path, const char *out_path, uint32_t *mparts_before, uint32_t *mparts_after);
+/* Writes the design with the micro-partition transforms tgs_init applies by
+ * default: lane packing (as tgs_pack_design) and then, with fast_luts, the
+ * regrouping of every exec level's single-level LUT micro-partitions by kind
+ * (ops with a word-wide form first, then ops that need table lookups; see
+ * tgs_options.fast_luts).  Same format, same values: any evaluator, the CPU
+ * oracle included, can check it.  No counterpart in the reference.  stats
+ * (optional) receives the micro-partition counts and the LUT ops (lutIndex
+ * != 0) that the device image evaluates word-wide. */
+typedef struct tgs_repack_stats {
+  uint64_t mparts_before, mparts_after;
+  uint64_t lut_ops;        /* LUT ops with lutIndex != 0 */
+  uint64_t fast_lut_ops;   /* of which evaluated with word-wide logic */
+  uint64_t fast_mparts;    /* micro-partitions whose top level is word-wide */
+  uint64_t reserved[3];
+} tgs_repack_stats;
+int tgs_repack_design(const char *in_path, const char *out_path, int lane_packing, int fast_luts,
+                      tgs_repack_stats *stats);
 
 #ifdef __cplusplus
 }

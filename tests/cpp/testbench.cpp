@@ -2,7 +2,8 @@
 // (toucanGPUSim::ToucanSimulator, include/ToucanGPUSim.h:10-74, and the
 // SimEval.h free functions, include/SimEval.h:21-40), built against this
 // library.  Usage: testbench <design.bin> <symbols.bin> <eval cycles> <free cycles>
-// Prints "name=value" for every register after the run, sorted by name.
+// Prints "name=value" for every register after the run, sorted by name;
+// built with ENABLE_SIM_PROFILE it then prints the per-partition profile.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -33,5 +34,9 @@ int main(int argc, char **argv) {
   std::printf("#read_reg_from_gpu=%llu\n", (unsigned long long)read_reg_from_gpu(locs));
   std::printf("#cycle_cnt=%llu real_cycles=%u stop=%d eval_done=%d\n", (unsigned long long)sim.cycle_cnt,
               get_real_cycles(), int(stop), int(get_eval_done()));
+#ifdef ENABLE_SIM_PROFILE
+  // the reference driver's profile report after a free-running call (main.cpp:62-64)
+  sim.printProfile();
+#endif
   return 0;
 }

@@ -69,3 +69,21 @@ def test_testbench_matches_oracle(tmp_path, small_design):
                     exp = (exp << 4) | int(regs[8 * k + j])
             assert int(val) == exp, name
     assert "#cycle_cnt=57 real_cycles=50" in r.stdout
+
+
+@pytest.mark.gpu
+def test_testbench_print_profile(tmp_path, small_design):
+    """ToucanSimulator::printProfile after eval_free_running (the reference's
+    profiling hook, src/ToucanSim.cu:307-315 over src/SimEval.cu:894-983):
+    one line per partition with 0 < useful ticks <= total ticks."""
+    dp, sp, info = small_design
+    exe = _compile(ROOT / "tests" / "cpp" / "testbench.cpp", tmp_path / "tbp", ["-DENABLE_SIM_PROFILE"])
+    r = subprocess.run([str(exe), str(dp), str(sp), "2", "250"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("Part ")]
+    assert len(lines) == info["partitions"], r.stdout[-2000:]
+    for l in lines:
+        # "Part p, useful X%, ticks U, total ticks T"
+        f = l.replace(",", "").split()
+        useful, total = int(f[5]), int(f[8])
+        assert 0 < useful <= total, l

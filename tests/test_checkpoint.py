@@ -68,3 +68,27 @@ def test_checkpoint_of_another_design_is_refused(design, tmp_path_factory, tmp_p
         (tmp_path / "junk.bin").write_bytes(b"not a state file at all, nope.")
         with pytest.raises(capi.TgsError):
             s2.load_state(tmp_path / "junk.bin")
+
+
+def test_truncated_checkpoint_leaves_handle_unchanged(design, tmp_path):
+    """A state file shorter than its header announces is refused before the
+    handle is reconfigured: stream count and state stay as they were."""
+    dp, sp, info = design
+    stim = sim.StimulusSpec(5, info["pi_ids"], info["pi_bits"])
+    with sim.Simulator(n_streams=24) as s:
+        s.init(0, dp, sp, True, False)
+        s.batch_run(np.full(24, 9, np.uint32), stim)
+        s.dump_state(tmp_path / "ck.bin")
+    raw = (tmp_path / "ck.bin").read_bytes()
+    (tmp_path / "short.bin").write_bytes(raw[:-1])
+    (tmp_path / "long.bin").write_bytes(raw + b"\0")
+    with sim.Simulator(n_streams=8) as s2:
+        s2.init(0, dp, sp, True, False)
+        s2.batch_run(np.full(8, 5, np.uint32), stim)
+        before = [s2.digest(k) for k in range(8)]
+        for name in ("short.bin", "long.bin"):
+            with pytest.raises(capi.TgsError) as e:
+                s2.load_state(tmp_path / name)
+            assert e.value.code == capi.ERR_FORMAT
+            assert s2.options()["n_streams"] == 8
+            assert [s2.digest(k) for k in range(8)] == before

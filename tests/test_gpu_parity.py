@@ -226,3 +226,53 @@ def test_digest_matches_host(designs):
             r, m = s.digest(stream)
             assert r == pyoracle.digest(s.reg_pool(stream))
             assert m == pyoracle.digest(s.mem_pool(stream))
+
+
+def test_read_registers_matches_oracle(designs):
+    """Every register of the symbol file, read after a run for several
+    streams: tgs_read_registers (one gather and one copy for all names) and
+    tgs_read_register equal the oracle's register pools, most significant
+    nibble first."""
+    dp, sp, info = designs["wide3op"]
+    regs = sim.symbol_registers(sp)
+    names = sorted(n for n in regs if len(regs[n]) <= 16)  # at most 64 bits (SimEval.cu:1062)
+    cycles = np.full(16, 21, np.uint32)
+    stim = _stim(info, seed=41)
+    ref = pyoracle.OracleDesign(dp, sp).run(cycles, stim, final_state=True)
+    with sim.Simulator(n_streams=16) as s:
+        s.init(0, dp, sp, False, False)
+        s.batch_run(cycles, stim)
+        for stream in (0, 5, 15):
+            pool = ref["final_regs"][stream]
+            expect = []
+            for n in names:
+                v = 0
+                for rid, _w in regs[n]:
+                    v = (v << 4) | int(pool[rid])
+                expect.append(v)
+            assert s.read_registers(names, stream=stream) == expect
+            for n, e in list(zip(names, expect))[:: max(1, len(names) // 16)]:
+                assert s.read_register(n, stream=stream) == e
+        assert s.read_registers([]) == []
+        with pytest.raises(sim.capi.TgsError) as e:
+            s.read_registers([names[0], "no_such_reg"])
+        assert e.value.code == sim.capi.ERR_NOT_FOUND
+
+
+@pytest.mark.parametrize("name", ["small", "mixed"])
+def test_copy_profile_data(designs, name):
+    """tgs_copy_profile_data (copy_profile_data, src/SimEval.cu:1101-1104):
+    after a free-running call of at least 200 cycles every partition has a
+    mean useful tick count in (0, total], totals covering the partition's
+    region (src/SimEval.cu:894-983); values stay bit-exact."""
+    dp, sp, _ = designs[name]
+    od = pyoracle.OracleDesign(dp, sp, randomize=True)
+    st = pyoracle.OracleState(od)
+    with sim.Simulator() as s:
+        s.init(0, dp, sp, True, False)
+        s.eval_free_running(230)
+        n = od.n_parts
+        useful, total = s.profile(n)
+        assert (useful > 0).all() and (useful <= total).all(), (useful[:8], total[:8])
+        st.eval(230)
+        np.testing.assert_array_equal(s.reg_pool(), st.regs())

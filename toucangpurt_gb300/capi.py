@@ -40,7 +40,7 @@ class Options(C.Structure):
         ("blocks_per_sm", C.c_uint32), ("schedule", C.c_uint32), ("mode", C.c_uint32),
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
         ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("lane_packing", C.c_uint32),
-        ("reserved", C.c_uint32 * 4),
+        ("fast_luts", C.c_uint32), ("reserved", C.c_uint32 * 3),
     ]
 
 
@@ -126,6 +126,11 @@ MLP_PARAMS = 5313
 
 # (name, argtypes) of every exported entry point; all return int status
 # except tgs_last_error / tgs_version.
+class RepackStats(C.Structure):
+    _fields_ = [("mparts_before", C.c_uint64), ("mparts_after", C.c_uint64), ("lut_ops", C.c_uint64),
+                ("fast_lut_ops", C.c_uint64), ("fast_mparts", C.c_uint64), ("reserved", C.c_uint64 * 3)]
+
+
 SIGNATURES = {
     "tgs_create": [C.POINTER(C.c_void_p)],
     "tgs_destroy": [C.c_void_p],
@@ -142,6 +147,7 @@ SIGNATURES = {
     "tgs_read_register": [C.c_void_p, C.c_char_p, u64p],
     "tgs_set_register_stream": [C.c_void_p, C.c_uint32, C.c_char_p, C.c_uint64],
     "tgs_read_register_stream": [C.c_void_p, C.c_uint32, C.c_char_p, u64p],
+    "tgs_read_registers": [C.c_void_p, C.c_uint32, C.POINTER(C.c_char_p), C.c_uint32, u64p],
     "tgs_read_signal": [C.c_void_p, C.c_char_p, u64p],
     "tgs_get_real_cycles": [C.c_void_p, u32p],
     "tgs_get_cycle_cnt": [C.c_void_p, u64p],
@@ -175,6 +181,7 @@ SIGNATURES = {
     "tgs_validate_file": [C.c_char_p, C.c_char_p, u64p],
     "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_pack_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
+    "tgs_repack_design": [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(RepackStats)],
     "tgs_dump_state": [C.c_void_p, C.c_char_p],
     "tgs_read_signal_stream": [C.c_void_p, C.c_uint32, C.c_char_p, C.POINTER(C.c_uint64)],
     "tgs_enable_vcd": [C.c_void_p, C.c_char_p],

@@ -114,6 +114,13 @@ __global__ void pokeRegsKernel(uint32_t *__restrict__ regs, uint32_t gpad, uint3
   }
 }
 
+// The nibbles of the listed register ids of one stream (readRegister).
+__global__ void peekRegsKernel(const uint32_t *__restrict__ regs, uint32_t gpad, uint32_t g, uint32_t k,
+                               const uint32_t *__restrict__ ids, uint8_t *__restrict__ out, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = uint8_t(nib(regs[size_t(ids[i]) * gpad + g], k));
+}
+
 }  // namespace
 
 void *cycleKernelFor(int spw, int G, bool resident) {
@@ -214,6 +221,13 @@ cudaError_t launchGatherRegs(const uint32_t *regs, uint32_t slots, uint32_t gpad
 cudaError_t launchScatterRegs(uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t g, uint32_t k, const uint8_t *in,
                               cudaStream_t st) {
   scatterRegsKernel<<<std::max<uint32_t>(1, std::min<uint32_t>(1024, (slots + 255) / 256)), 256, 0, st>>>(regs, slots, gpad, g, k, in);
+  return cudaGetLastError();
+}
+
+cudaError_t launchPeekRegs(const uint32_t *regs, uint32_t gpad, uint32_t g, uint32_t k, const uint32_t *ids,
+                           uint8_t *out, uint32_t n, cudaStream_t st) {
+  if (!n) return cudaSuccess;
+  peekRegsKernel<<<std::max<uint32_t>(1, std::min<uint32_t>(1024, (n + 255) / 256)), 256, 0, st>>>(regs, gpad, g, k, ids, out, n);
   return cudaGetLastError();
 }
 

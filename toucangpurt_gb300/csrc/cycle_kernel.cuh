@@ -230,6 +230,43 @@ __device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t sr
   }
 }
 
+// ---- word-wide top-level ops (records with kMPFastTop) ----------------------
+// The op's table row is a bitwise function g of (b, c) -- checked against the
+// table at load time -- so the 8 streams of a word take
+//   out = Q ^ (C & (P ^ Q)),  P = g01 ^ (B & (g11 ^ g01)),  Q = g00 ^ (B & (g10 ^ g00))
+// (g_xy: all ones where g(x, y) = 1), three bitwise instructions.  A
+// multiplexer (kind 1: a ? b : c, kind 2: a ? c : b) starts from the pass-c
+// (pass-b) row and blends in the other operand where the select nibble is 1;
+// a word with a select nibble above 1 reads the table window instead.
+template <int SPW, int H>
+__device__ __forceinline__ void fastTop(uint32_t tab, uint32_t lut, const uint32_t (&A)[H], const uint32_t (&B)[H],
+                                        const uint32_t (&C)[H], uint32_t (&v)[H], bool anySel) {
+  const bool isFast = (lut & kFastOp) != 0;
+  const uint32_t kind = isFast ? (lut >> kFastKindShift) & 3u : 0u;
+  const uint32_t g = !isFast ? kGPassC : kind == 0u ? (lut & 15u) : kind == 1u ? kGPassC : kGPassB;
+  const uint32_t g00 = 0u - (g & 1u), g01 = 0u - ((g >> 1) & 1u), g10 = 0u - ((g >> 2) & 1u), g11 = 0u - (g >> 3);
+  const uint32_t k1 = g11 ^ g01, k0 = g10 ^ g00;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const uint32_t P = (B[i] & k1) ^ g01, Q = (B[i] & k0) ^ g00;
+    v[i] = Q ^ (C[i] & (P ^ Q));
+  }
+  if (anySel && kind != 0u) {
+    // select nibbles: 0 or 1 in every stream of the word (SPW = 1: nibble 0)
+    constexpr uint32_t kHigh = SPW == 8 ? 0xEEEEEEEEu : 0xEu;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      if ((A[i] & kHigh) == 0u) {
+        const uint32_t m = (A[i] & 0x11111111u) * 15u;
+        const uint32_t X = kind == 1u ? B[i] : C[i];
+        v[i] ^= m & (X ^ v[i]);
+      } else {
+        v[i] = lookup<SPW>(tab, lut & 0x1FFFu, A[i], B[i], C[i]);
+      }
+    }
+  }
+}
+
 // ---- micro-partitions (evalSingleMicroPart, SimEval.cu:304-580) -----------
 // One pass of a LUT micro-partition over H stream groups starting at group
 // h0 of the item (value-pool words [slot][G]).
@@ -244,8 +281,14 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
     const uint2 t = top.pair(2u * lane);
     const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
     uint32_t A[H], B[H], C[H];
+    // a word-wide record without multiplexers never reads op0
+    const bool needA = (hdr & (kMPFastTop | kMPFastSel)) != kMPFastTop;
     if (constSlots) {
-      loadG<H>(vpAddr<G>(vp, a, h0), A);
+      if (needA) loadG<H>(vpAddr<G>(vp, a, h0), A);
+      else {
+#pragma unroll
+        for (int g = 0; g < H; ++g) A[g] = 0u;
+      }
       loadG<H>(vpAddr<G>(vp, b, h0), B);
       loadG<H>(vpAddr<G>(vp, c, h0), C);
     } else {
@@ -268,8 +311,12 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
         loadG<H>(vpAddr<G>(vp, c, h0), C);
       }
     }
+    if (hdr & kMPFastTop) {
+      fastTop<SPW, H>(tab, lut, A, B, C, v, (hdr & kMPFastSel) != 0);
+    } else {
 #pragma unroll
-    for (int g = 0; g < H; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
+      for (int g = 0; g < H; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];
+    }
   } else {
 #pragma unroll
     for (int g = 0; g < H; ++g) v[g] = 0;

@@ -23,7 +23,10 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 
 // Header word: kind | lanes(6) << 2 | nMid(8) << 8 | nWB(6) << 16 | nTop(6) << 24
 // | direct write-back << 30 (LUT: write-back entry l takes lane l's result,
-// shuffleId == 32 + l for every entry, so no lane exchange is needed).
+// shuffleId == 32 + l for every entry, so no lane exchange is needed)
+// | fast top level << 31 (every top-level op has a word-wide form: its lut
+// field holds the fast code of emit.h, not a table offset) | some fast op is
+// a multiplexer << 23.
 // LUT micro-partition words after the 4-word header (all lane-major):
 //   top:  2 * W words, lane l: [lutIndex | op0 << 16, op1 | op2 << 16] (zero for idle lanes)
 //   mid:  nMid * W words, the reference's packed middle-level op (zero = move of immediate 0)
@@ -35,6 +38,17 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 //   MemRead (4 words): memBase lo, memBase hi | multiWriter << 31, en | addrVec << 16, result
 constexpr uint32_t kMPHeaderWords = 4;
 constexpr uint32_t kMPDirectWB = 1u << 30;
+constexpr uint32_t kMPFastTop = 1u << 31, kMPFastSel = 1u << 23;
+// Top-level lut field of a word-wide ("fast") op, in a record with kMPFastTop:
+//   kFastOp | kind << kFastKindShift | payload
+//   kind 0: out = g(b, c) bit by bit, payload = g (bit (x << 1 | y) = g(b bit
+//           x, c bit y));  kind 1: out = a ? b : c;  kind 2: out = a ? c : b
+//   (kinds 1 and 2 for select nibbles 0 and 1; payload = lutIndex, the table
+//   window a word with another select value reads).
+// A lut field without kFastOp in such a record is a move or an idle lane
+// (out = c).
+constexpr uint32_t kFastOp = 0x8000u, kFastKindShift = 13;
+constexpr uint32_t kGPassC = 0xAu, kGPassB = 0xCu;  // g of "c" and of "b"
 constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;
 // schedule unit word: record offset (words from the level block) | first
 // group << 24 | (groups - 1) << 27

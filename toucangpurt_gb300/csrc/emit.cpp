@@ -27,7 +27,56 @@ void align4(std::vector<uint32_t> &v) {
   while (v.size() % 4) v.push_back(0);
 }
 
-uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f) {
+}  // namespace
+
+// ---- word-wide evaluation of palette LUT ops -------------------------------
+FastLuts::FastLuts(const std::vector<uint8_t> &lut) : lut_(lut), rowCode_(lut.size(), -2), muxCode_(lut.size(), -2) {}
+
+// The 2-input function of a 256-entry row (index b << 4 | c), as the 4-bit
+// truth table g of one output bit (bit (x << 1 | y) = g(b bit x, c bit y)),
+// when every entry is that function applied to each of the 4 bits; else -1.
+int FastLuts::rowCode(uint32_t row) {
+  if (row + 256 > lut_.size()) return -1;
+  int &memo = rowCode_[row];
+  if (memo != -2) return memo;
+  memo = -1;
+  const uint32_t v01 = lut_[row + 0x0F], v10 = lut_[row + 0xF0], v11 = lut_[row + 0xFF], v00 = lut_[row];
+  for (uint32_t v : {v00, v01, v10, v11})
+    if (v != 0 && v != 15) return memo;
+  const uint32_t g = (v00 & 1u) | ((v01 & 1u) << 1) | ((v10 & 1u) << 2) | ((v11 & 1u) << 3);
+  for (uint32_t b = 0; b < 16; ++b)
+    for (uint32_t c = 0; c < 16; ++c) {
+      uint32_t want = 0;
+      for (uint32_t i = 0; i < 4; ++i) want |= ((g >> ((((b >> i) & 1u) << 1) | ((c >> i) & 1u))) & 1u) << i;
+      if (lut_[row + (b << 4 | c)] != want) return memo;
+    }
+  return memo = int(g);
+}
+
+// A 4,096-entry window whose rows a = 0 and a = 1 pass one operand each: 1
+// for a ? b : c, 2 for a ? c : b, else 0.
+int FastLuts::muxCode(uint32_t base) {
+  if (base >= 1u << 13 || base + 4096 > lut_.size()) return 0;
+  int &memo = muxCode_[base];
+  if (memo != -2) return memo;
+  const int r0 = rowCode(base), r1 = rowCode(base + 256);
+  memo = r0 == kGPassC && r1 == kGPassB ? 1 : r0 == kGPassB && r1 == kGPassC ? 2 : 0;
+  return memo;
+}
+
+uint16_t FastLuts::code(const CGMicroPartLUTTopLevelOp &o) {
+  if (o.lutIndex == 0) return uint16_t(kFastOp | kGPassC);  // a move passes op2
+  if (o.op0 < 16) {
+    const int g = rowCode(uint32_t(o.lutIndex) + (uint32_t(o.op0) << 8));
+    return g < 0 ? 0 : uint16_t(kFastOp | uint32_t(g));
+  }
+  const int k = muxCode(o.lutIndex);
+  return k ? uint16_t(kFastOp | (uint32_t(k) << kFastKindShift) | o.lutIndex) : 0;
+}
+
+namespace {
+
+uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f, FastLuts *fast) {
   uint32_t W = uint32_t(m.topLevel.size());
   for (auto &l : m.middleLevels) W = std::max<uint32_t>(W, uint32_t(l.size()));
   W = std::max<uint32_t>(W, uint32_t(m.lastLevel.size()));
@@ -35,17 +84,27 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
   uint32_t nMid = uint32_t(m.middleLevels.size());
   bool direct = true;
   for (size_t l = 0; l < m.lastLevel.size(); ++l) direct = direct && m.lastLevel[l].shuffleId == 32 + l;
+  // word-wide top level: every top op (and idle lane) has a fast form
+  std::vector<uint16_t> codes;
+  bool fastTop = fast != nullptr && !m.topLevel.empty(), sel = false;
+  for (size_t l = 0; fastTop && l < m.topLevel.size(); ++l) {
+    codes.push_back(fast->code(m.topLevel[l]));
+    fastTop = codes.back() != 0;
+    sel = sel || ((codes.back() >> kFastKindShift) & 3u) != 0;
+  }
   align4(net);
   uint32_t off = uint32_t(net.size());
   net.push_back(kMPLut | (W << 2) | (nMid << 8) | (uint32_t(m.lastLevel.size()) << 16) |
-                (uint32_t(m.topLevel.size()) << 24) | (direct ? kMPDirectWB : 0u));
+                (uint32_t(m.topLevel.size()) << 24) | (direct ? kMPDirectWB : 0u) | (fastTop ? kMPFastTop : 0u) |
+                (fastTop && sel ? kMPFastSel : 0u));
   net.push_back(0);
   net.push_back(0);
   net.push_back(0);
   for (uint32_t l = 0; l < W; ++l) {
     if (l < m.topLevel.size()) {
       const auto &o = m.topLevel[l];
-      net.push_back(uint32_t(o.lutIndex) | (uint32_t(o.op0) << 16));
+      net.push_back(uint32_t(fastTop ? codes[l] : o.lutIndex) | (uint32_t(o.op0) << 16));
+      f.fastOps += fastTop && o.lutIndex != 0;
       net.push_back(uint32_t(o.op1) | (uint32_t(o.op2) << 16));
       f.ops += 1;
       f.nops += o.lutIndex == 0;
@@ -186,6 +245,98 @@ std::vector<CGMicroPartInfo> packLevel(const std::vector<CGMicroPartInfo> &in) {
   return res;
 }
 
+// Regrouping of single-level LUT micro-partitions (see emit.h).
+std::vector<CGMicroPartInfo> regroupLevel(const std::vector<CGMicroPartInfo> &in, FastLuts *fast) {
+  std::vector<uint32_t> cand;
+  for (uint32_t i = 0; i < in.size(); ++i)
+    if (in[i].isLUTPart && in[i].middleLevels.empty() && !in[i].lastLevel.empty()) cand.push_back(i);
+  if (cand.empty()) return in;
+  struct Item {
+    CGMicroPartLUTTopLevelOp op;
+    std::vector<uint16_t> results;  // slots that take the op's value
+    uint32_t cls;                   // 0 word-wide, 1 word-wide multiplexer, 2 table
+  };
+  std::vector<Item> items;
+  std::vector<std::pair<uint8_t, uint16_t>> imm;  // (immediate value, slot)
+  std::vector<int32_t> writer;                    // slot -> item (or -2 for an immediate), -1 none
+  std::vector<uint8_t> readSlot;
+  auto grow = [&](uint32_t s) {
+    if (s >= writer.size()) {
+      writer.resize(s + 1, -1);
+      readSlot.resize(s + 1, 0);
+    }
+  };
+  // the value an entry takes: (item, -1) for a lane, (-1, value) for an immediate
+  for (uint32_t i : cand) {
+    const CGMicroPartInfo &m = in[i];
+    const uint32_t base = uint32_t(items.size()), nTop = uint32_t(m.topLevel.size());
+    for (auto &o : m.topLevel) {
+      const uint16_t code = fast ? fast->code(o) : 0;
+      const uint32_t cls = code == 0 ? 2u : ((code >> kFastKindShift) & 3u) ? 1u : 0u;
+      items.push_back({o, {}, cls});
+      for (uint16_t s : {o.op0, o.op1, o.op2})
+        if (s >= 16) {
+          grow(s);
+          readSlot[s] = 1;
+        }
+    }
+    for (auto &w : m.lastLevel) {
+      int32_t src = -2;  // immediate
+      uint8_t val = w.shuffleId;
+      if (w.shuffleId >= 32) {
+        const uint32_t lane = w.shuffleId & 31u;
+        if (lane < nTop) src = int32_t(base + lane);
+        else val = 0;  // an idle lane holds 0
+      }
+      grow(w.result);
+      if (writer[w.result] != -1) {
+        // the same value into the same slot again is harmless; anything else
+        // leaves the level as it is
+        const bool same = src >= 0 ? writer[w.result] == src
+                                   : writer[w.result] == -2 &&
+                                         std::any_of(imm.begin(), imm.end(), [&](auto &e) { return e.second == w.result && e.first == val; });
+        if (!same) return in;
+        continue;
+      }
+      writer[w.result] = src;
+      if (src >= 0) items[size_t(src)].results.push_back(w.result);
+      else imm.push_back({val, w.result});
+    }
+  }
+  for (size_t s = 0; s < writer.size(); ++s)
+    if (writer[s] != -1 && readSlot[s]) return in;  // an op reads a slot the level writes
+  for (const Item &it : items)
+    if (it.results.size() > 32) return in;  // more write-back entries than one micro-partition holds
+  std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.cls < b.cls; });
+  std::vector<CGMicroPartInfo> out;
+  for (uint32_t i = 0; i < in.size(); ++i)
+    if (!(in[i].isLUTPart && in[i].middleLevels.empty() && !in[i].lastLevel.empty())) out.push_back(in[i]);
+  CGMicroPartInfo cur;
+  uint32_t curCls = 0;
+  auto flush = [&]() {
+    if (!cur.topLevel.empty() || !cur.lastLevel.empty()) out.push_back(std::move(cur));
+    cur = CGMicroPartInfo();
+    cur.isLUTPart = true;
+  };
+  cur.isLUTPart = true;
+  for (const Item &it : items) {
+    const bool table = it.cls == 2;
+    if (!cur.topLevel.empty() && ((curCls == 2) != table || cur.topLevel.size() == 32 ||
+                                  cur.lastLevel.size() + it.results.size() > 32))
+      flush();
+    curCls = it.cls;
+    const uint8_t lane = uint8_t(32 + cur.topLevel.size());
+    cur.topLevel.push_back(it.op);
+    for (uint16_t r : it.results) cur.lastLevel.push_back({lane, r});
+  }
+  for (auto &e : imm) {
+    if (cur.lastLevel.size() == 32) flush();
+    cur.lastLevel.push_back({e.first, e.second});
+  }
+  flush();
+  return out;
+}
+
 namespace {
 
 uint32_t emitSpecial(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat &f) {
@@ -281,8 +432,11 @@ void accessOf(const CGMicroPartInfo &m, std::vector<uint32_t> &rd, std::vector<u
 
 }  // namespace
 
-void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, const ProbeList *probes, bool packLanes) {
+void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, const ProbeList *probes, bool packLanes,
+                bool fastLuts) {
   img = DeviceImage();
+  FastLuts fl(d.lut);
+  FastLuts *fast = fastLuts && d.lut.size() == kLutSize ? &fl : nullptr;
   img.parts.resize(d.parts.size());
   img.mp.resize(d.parts.size());
   img.partRegion.assign(d.parts.size(), 0);
@@ -333,10 +487,11 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, con
     for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
       std::vector<CGMicroPartInfo> packed;
       if (packLanes) packed = packLevel(p.exec_mParts[lv]);
-      for (const auto &m : packLanes ? packed : p.exec_mParts[lv]) {
+      if (fast) packed = regroupLevel(packLanes ? packed : p.exec_mParts[lv], fast);
+      for (const auto &m : (packLanes || fast) ? packed : p.exec_mParts[lv]) {
         MPartRef ref;
         ref.feat.partLevels = pd.nLevels;
-        ref.off = m.isLUTPart ? emitLut(m, net, ref.feat) : emitSpecial(m, net, ref.feat);
+        ref.off = m.isLUTPart ? emitLut(m, net, ref.feat, fast) : emitSpecial(m, net, ref.feat);
         ref.words = uint32_t((net.size() + 3) / 4 * 4) - ref.off;
         ref.id = img.nMParts++;
         net[ref.off + 1] = ref.id;  // header word 1: design-wide micro-partition id (profiling)

@@ -24,6 +24,7 @@ struct MPartFeat {
   uint32_t fanIn = 0;       // distinct slots read
   uint32_t fanOut = 0;      // later readers of its outputs
   uint32_t partLevels = 0;  // exec levels of its partition
+  uint32_t fastOps = 0;     // LUT ops evaluated with word-wide logic (no table read)
 };
 
 struct MPartRef {
@@ -61,6 +62,42 @@ struct Schedule {
   uint64_t barriers = 0, levels = 0;
 };
 
+// Word-wide evaluation of palette LUT ops.  A LUT op reads table entry
+// lutIndex + (a << 8 | b << 4 | c) per stream (src/SimEval.cu:350-356).
+// When a is an immediate and the 256 entries of that row are a bitwise
+// function g of (b, c) -- every output bit i equal to g(b_i, c_i): AND, OR,
+// XOR, NAND, a move ... -- the kernel computes the 8 streams of a word with
+// three bitwise instructions instead of eight table reads.  When a is a slot
+// and rows a = 0 and a = 1 pass c and b (a multiplexer) or b and c, the word
+// is c ^ (mask(a) & (b ^ c)) whenever every stream's a is 0 or 1; a word with
+// another select value reads the table.  Every entry of a row is compared
+// with the function at load time, so results equal the table lookups.
+//
+// The device image's encoding of fast ops: kFastOp and friends (devimage.h).
+
+class FastLuts {
+ public:
+  explicit FastLuts(const std::vector<uint8_t> &lut);
+  // the op's fast lut field, or 0 when it needs table lookups
+  uint16_t code(const toucanGPUSim::CGMicroPartLUTTopLevelOp &o);
+  int rowCode(uint32_t row);
+  int muxCode(uint32_t base);
+
+ private:
+  const std::vector<uint8_t> &lut_;
+  std::vector<int> rowCode_, muxCode_;  // -2: not computed yet
+};
+
+// One exec level with its single-level LUT micro-partitions (top level and
+// write-back only) regrouped op by op: ops with a fast form first, then ops
+// that need table lookups, each group packed into micro-partitions of up to
+// 32 lanes and 32 write-back entries, so that a warp evaluates ops of one
+// kind.  Ops of such micro-partitions are independent (each reads slots no
+// op of the level writes), which is checked; a level that breaks it is
+// returned unchanged.  fast == nullptr: repacked in op order.
+std::vector<toucanGPUSim::CGMicroPartInfo> regroupLevel(const std::vector<toucanGPUSim::CGMicroPartInfo> &in,
+                                                       FastLuts *fast);
+
 // compactSlots: renumber value-pool slots by live range (slotalloc.h).
 // probes (optional): per partition, (value-pool slot, probe index) pairs
 // whose values the kernel records after the exec levels (signal capture).
@@ -69,9 +106,11 @@ using ProbeList = std::vector<std::vector<std::pair<uint32_t, uint32_t>>>;
 // side into 32-lane ones (same values; emit.cpp).
 std::vector<toucanGPUSim::CGMicroPartInfo> packLevel(const std::vector<toucanGPUSim::CGMicroPartInfo> &in);
 
-// packLanes: packLevel applied to every exec level.
+// packLanes: packLevel applied to every exec level; fastLuts: palette ops
+// evaluated word-wide, single-level micro-partitions regrouped by kind
+// (after packing).
 void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool compactSlots,
-                const ProbeList *probes = nullptr, bool packLanes = false);
+                const ProbeList *probes = nullptr, bool packLanes = false, bool fastLuts = false);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
 // G: stream groups per item (special micro-partitions are split by group).
 void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,

@@ -36,6 +36,8 @@ cudaError_t launchGatherRegs(const uint32_t *regs, uint32_t slots, uint32_t gpad
                              cudaStream_t st);
 cudaError_t launchScatterRegs(uint32_t *regs, uint32_t slots, uint32_t gpad, uint32_t g, uint32_t k, const uint8_t *in,
                               cudaStream_t st);
+cudaError_t launchPeekRegs(const uint32_t *regs, uint32_t gpad, uint32_t g, uint32_t k, const uint32_t *ids,
+                           uint8_t *out, uint32_t n, cudaStream_t st);
 cudaError_t launchPokeRegs(uint32_t *regs, uint32_t gpad, uint32_t g, uint32_t k, const uint32_t *ids,
                            const uint8_t *vals, uint32_t n, cudaStream_t st);
 

@@ -9,7 +9,7 @@
 // (every GPU that loads the library holds it until exit).
 #include <cuda_runtime.h>
 
-#include <mutex>
+#include <new>
 #include <string>
 
 #include "kernels.h"
@@ -19,28 +19,19 @@ namespace tgs {
 namespace {
 
 constexpr uint32_t kNoAllocMaxPools = 4096;  // 32 KiB of accumulators per device
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned long long gPoolDigestScratch[kNoAllocMaxPools];
 
-std::mutex gScratchMu;
-unsigned long long *gScratchAddr[kMaxDevices] = {};
-
-// Device address of the accumulator array on the current device; resolved
-// once per device (with that device current) on its first call.
+// Device address of the accumulator array in the current device's context.
+// Resolved on every call, with that device current: the lookup allocates
+// nothing, and a context the caller re-created (cudaDeviceReset) places the
+// array at a new address that a cached pointer would miss.  The first call
+// on a device loads the library's device code into its context.
 unsigned long long *scratchForCurrentDevice() {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) throw Error(TGS_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) throw Error(TGS_ERR_NO_DEVICE, "device ordinal beyond 63");
-  std::lock_guard<std::mutex> g(gScratchMu);
-  if (!gScratchAddr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, gPoolDigestScratch);
-    if (e != cudaSuccess) throw Error(TGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    gScratchAddr[dev] = static_cast<unsigned long long *>(p);
-  }
-  return gScratchAddr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, gPoolDigestScratch);
+  if (e != cudaSuccess) throw Error(TGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  return static_cast<unsigned long long *>(p);
 }
 
 }  // namespace
@@ -68,5 +59,11 @@ extern "C" int tgs_pool_digests_noalloc(const uint8_t *pools, uint64_t stride, u
   } catch (const Error &err) {
     setLastError(err.what());
     return err.code;
+  } catch (const std::bad_alloc &) {
+    setLastError("host out of memory");
+    return TGS_ERR_RESOURCES;
+  } catch (const std::exception &err) {
+    setLastError(err.what());
+    return TGS_ERR_ARG;
   }
 }

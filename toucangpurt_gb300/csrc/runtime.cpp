@@ -515,7 +515,7 @@ void upload(tgs_sim *h) {
   cudaStream_t s = h->stream;
   buildProbes(h);
   buildImage(h->design, h->img, h->opt.value_pool == 0, h->captureSignals ? &h->probes : nullptr,
-             h->opt.lane_packing == 0);
+             h->opt.lane_packing == 0, h->opt.fast_luts == 0);
   h->net.upload(h->img.net, s);
   h->constVec.upload(h->img.constVec, s);
   std::vector<uint8_t> lut(kLutTablePadded, 0);
@@ -826,17 +826,42 @@ void vcdDump(tgs_sim *h, uint64_t cycle) {
   o.flush();
 }
 
-uint64_t readRegister(tgs_sim *h, uint32_t s, const char *name) {
-  const auto &locs = regLocs(h, name);
+// read_reg_from_gpu (SimEval.cu:1058-1069), most significant nibble first,
+// for many registers at once: the nibbles of every listed register are
+// gathered by one kernel and read back with one copy (the reference copies
+// one byte per nibble, each a blocking cudaMemcpy).
+void readRegisters(tgs_sim *h, uint32_t s, const char *const *names, uint32_t n, uint64_t *out) {
+  if (n && (!names || !out)) throw Error(TGS_ERR_ARG, "null names or values");
+  std::vector<uint32_t> ids, first(n + 1, 0);
+  for (uint32_t i = 0; i < n; ++i) {
+    first[i] = uint32_t(ids.size());
+    for (auto &l : regLocs(h, names[i])) {
+      const uint32_t id = std::get<0>(l);
+      if (id >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "register id beyond regPool");
+      ids.push_back(id);
+    }
+  }
+  first[n] = uint32_t(ids.size());
   uint32_t g, k;
   streamPos(h, s, g, k);
-  uint64_t r = 0;
-  for (auto &l : locs) {
-    uint32_t id = std::get<0>(l), w = 0;
-    if (id >= h->design.regPoolSize) throw Error(TGS_ERR_RANGE, "register id beyond regPool");
-    TGS_CUDA(cudaMemcpy(&w, h->regs.p + size_t(id) * h->gpad + g, 4, cudaMemcpyDeviceToHost));
-    r = (r << 4) | ((w >> (4 * k)) & 0xF);
+  std::vector<uint8_t> nibs(ids.size());
+  if (!ids.empty()) {
+    h->ioIds.upload(ids, h->stream);
+    if (h->ioBytes.n < ids.size()) h->ioBytes.alloc(ids.size());
+    TGS_CUDA(launchPeekRegs(h->regs.p, h->gpad, g, k, h->ioIds.p, h->ioBytes.p, uint32_t(ids.size()), h->stream));
+    TGS_CUDA(cudaMemcpyAsync(nibs.data(), h->ioBytes.p, nibs.size(), cudaMemcpyDeviceToHost, h->stream));
+    TGS_CUDA(cudaStreamSynchronize(h->stream));
   }
+  for (uint32_t i = 0; i < n; ++i) {
+    uint64_t r = 0;
+    for (uint32_t j = first[i]; j < first[i + 1]; ++j) r = (r << 4) | (nibs[j] & 0xFu);
+    out[i] = r;
+  }
+}
+
+uint64_t readRegister(tgs_sim *h, uint32_t s, const char *name) {
+  uint64_t r = 0;
+  readRegisters(h, s, &name, 1, &r);
   return r;
 }
 
@@ -1081,6 +1106,13 @@ int tgs_read_register_stream(tgs_sim *h, uint32_t s, const char *name, uint64_t 
   });
 }
 
+int tgs_read_registers(tgs_sim *h, uint32_t stream, const char *const *names, uint32_t n, uint64_t *values) {
+  return guard([&] {
+    requireLoaded(h);
+    readRegisters(h, stream, names, n, values);
+  });
+}
+
 int tgs_read_signal(tgs_sim *h, const char *name, uint64_t *value) {
   return guard([&] {
     requireLoaded(h);
@@ -1301,6 +1333,18 @@ int tgs_load_state(tgs_sim *h, const char *path) {
       throw Error(TGS_ERR_ARG, "state file of another design");
     if (hd.nStreams == 0) throw Error(TGS_ERR_FORMAT, "state file without streams");
     const uint32_t n = hd.nStreams;
+    // the file must hold every stream the header announces before the
+    // handle is reconfigured or its state touched: a truncated or corrupt
+    // file leaves the handle as it was
+    {
+      const std::streampos here = in.tellg();
+      in.seekg(0, std::ios::end);
+      const uint64_t size = uint64_t(in.tellg());
+      in.seekg(here);
+      const uint64_t perStream = 16ull + hd.regPoolSize + hd.memPoolSize;
+      if (!in || n > (size - sizeof(StateHeader)) / perStream || size != sizeof(StateHeader) + uint64_t(n) * perStream)
+        throw Error(TGS_ERR_FORMAT, "state file size does not match its header");
+    }
     std::vector<uint32_t> stop(n), stopCycle(n);
     std::vector<unsigned long long> roll(n);
     in.read(reinterpret_cast<char *>(stop.data()), n * 4ull);
@@ -1856,6 +1900,47 @@ extern "C" int tgs_pack_design(const char *in, const char *out, uint32_t *mparts
       }
     if (mparts_before) *mparts_before = before;
     if (mparts_after) *mparts_after = after;
+    std::ofstream o(out, std::ios::binary);
+    if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
+    serializeSimDesignInfo(o, d);
+  });
+}
+
+extern "C" int tgs_repack_design(const char *in, const char *out, int lanePacking, int fastLuts,
+                                 tgs_repack_stats *stats) {
+  return guard([&] {
+    if (!in || !out) throw Error(TGS_ERR_ARG, "null argument");
+    auto bytes = readFileBytes(in);
+    SimDesignInfo d;
+    parseDesign(bytes.data(), bytes.size(), d);
+    tgs_repack_stats st;
+    std::memset(&st, 0, sizeof st);
+    FastLuts fl(d.lut);
+    FastLuts *fast = fastLuts && d.lut.size() == kLutSize ? &fl : nullptr;
+    for (auto &p : d.parts)
+      for (auto &lvl : p.exec_mParts) {
+        st.mparts_before += lvl.size();
+        if (lanePacking) lvl = packLevel(lvl);
+        if (fast) lvl = regroupLevel(lvl, fast);
+        st.mparts_after += lvl.size();
+        for (auto &m : lvl) {
+          if (!m.isLUTPart) continue;
+          uint64_t luts = 0;
+          bool wordWide = fast && !m.topLevel.empty();
+          for (auto &o : m.topLevel) {
+            luts += o.lutIndex != 0;
+            wordWide = wordWide && fast->code(o) != 0;
+          }
+          for (auto &lv : m.middleLevels)
+            for (auto &o : lv) st.lut_ops += o.lutIndex() != 0;
+          st.lut_ops += luts;
+          if (wordWide) {
+            st.fast_lut_ops += luts;
+            st.fast_mparts += 1;
+          }
+        }
+      }
+    if (stats) *stats = st;
     std::ofstream o(out, std::ios::binary);
     if (!o) throw Error(TGS_ERR_IO, std::string("cannot write ") + out);
     serializeSimDesignInfo(o, d);

@@ -99,6 +99,13 @@ class Simulator:
         check(lib().tgs_read_register_stream(self._h, stream, name.encode(), C.byref(v)))
         return v.value
 
+    def read_registers(self, names, stream: int = 0) -> list[int]:
+        """Many registers of one stream with one gather and one copy back."""
+        arr = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+        out = np.zeros(max(1, len(names)), np.uint64)
+        check(lib().tgs_read_registers(self._h, stream, arr, len(names), _ptr(out, C.c_uint64)))
+        return [int(v) for v in out[: len(names)]]
+
     # reference spellings
     setRegister = set_register
     readRegister = read_register
@@ -329,11 +336,22 @@ def mix64(z: np.ndarray) -> np.ndarray:
         return z ^ (z >> np.uint64(31))
 
 
+def symbol_registers(symbol_path) -> dict:
+    """regDebugInfo of a symbol file: name -> [(register nibble id, width)],
+    most significant nibble first."""
+    return _symbol_maps(symbol_path)[0]
+
+
 def symbol_signals(symbol_path) -> dict:
     """signalDebugInfo of a symbol file: name -> [(partition, slot, width)],
-    most significant section first (host-side reader of the reference's
-    symbol format: three maps of u64 count, then per entry a u64-length
-    string, a u64 tuple count and u32 tuples)."""
+    most significant section first."""
+    return _symbol_maps(symbol_path)[1]
+
+
+def _symbol_maps(symbol_path):
+    """Register and signal maps of a symbol file (host-side reader of the
+    reference's symbol format: three maps of u64 count, then per entry a
+    u64-length string, a u64 tuple count and u32 tuples)."""
     import struct
 
     b = Path(symbol_path).read_bytes()
@@ -358,8 +376,8 @@ def symbol_signals(symbol_path) -> dict:
             out[key] = [tuple(vals[i:i + arity]) for i in range(0, len(vals), arity)]
         return out
 
-    read_map(2)  # registers
-    return read_map(3)
+    regs = read_map(2)
+    return regs, read_map(3)
 
 
 def stimulus_table(spec: StimulusSpec, n_streams: int, c0: int, cycles: int, out: np.ndarray | None = None,

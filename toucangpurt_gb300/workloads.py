@@ -82,3 +82,37 @@ def toggles(name: str, bits: np.ndarray) -> np.ndarray | None:
     else:
         t[bits == 1] = int(round(p * 65536))
     return t
+
+
+def bench_simulator(name: str, design, symbols, *, streams: int | None = None, gpu: int = 0, schedule: str = "auto",
+                    mode: str = "auto", groups: int = 0, warps: int = 0, levels: int = 0, value_pool: int = 0,
+                    profile_cycles: int = 20, epochs: int = 40, seed: int = 5, **options):
+    """A simulator loaded and configured the way the benchmark runs a
+    workload: `streams` resident streams (default: the workload's count),
+    the CUDA-graph form unless the exec levels stay resident in shared
+    memory (then one persistent launch), and for more than one stream the
+    learned schedule (every micro-partition profiled for `profile_cycles`
+    cycles, the cost model trained on those samples).  Further tgs_options
+    fields may be given by name.  Returns (simulator, notes) where notes
+    holds the cost model's validation figures."""
+    import time
+
+    from . import capi, sim
+
+    streams = streams or RUNS[name]["streams"]
+    if schedule == "auto":
+        schedule = "learned" if streams > 1 else "greedy"
+    s = sim.Simulator(n_streams=streams, groups_per_item=groups, warps_per_block=warps, resident_netlist=levels,
+                      mode=capi.MODE_PERSISTENT if mode == "persistent" else capi.MODE_GRAPH, value_pool=value_pool,
+                      **options)
+    s.init(gpu, design, symbols, False, False)
+    notes = {"schedule": schedule}
+    if mode == "auto" and s.design_stats().get("resident_words"):
+        s.set_options(mode=capi.MODE_PERSISTENT)  # resident levels are loaded once per run
+    if schedule == "learned":
+        t0 = time.perf_counter()
+        rep = s.train_cost_model(s.mpart_features(), s.profile_mparts(profile_cycles), epochs=epochs, seed=seed)
+        s.set_options(schedule=capi.SCHED_LEARNED)
+        notes["cost_model"] = {k: round(float(v), 4) for k, v in rep.items() if k in ("val_mse", "val_corr", "gate_corr")}
+        notes["cost_model"]["train_s"] = round(time.perf_counter() - t0, 2)
+    return s, notes
