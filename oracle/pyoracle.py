@@ -30,6 +30,14 @@ class Result(C.Structure):
                 ("final_regs", C.POINTER(C.c_uint8)), ("final_mems", C.POINTER(C.c_uint8))]
 
 
+def reference_dir() -> Path | None:
+    """The reference checkout the recipe (oracle/Makefile) builds from, or
+    None where it is absent."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref-dir"], capture_output=True, text=True)
+    d = Path(r.stdout.strip()) if r.returncode == 0 and r.stdout.strip() else None
+    return d if d is not None and d.is_dir() else None
+
+
 def build() -> None:
     r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
     if r.returncode != 0:

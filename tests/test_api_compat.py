@@ -11,8 +11,11 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle import pyoracle
+
 ROOT = Path(__file__).resolve().parents[1]
-REF_MAIN = Path("/root/reference/main.cpp")
+REF_DIR = pyoracle.reference_dir()  # where oracle/Makefile finds the reference checkout, or None
+REF_MAIN = REF_DIR / "main.cpp" if REF_DIR else None
 CUDA_INC = "/usr/local/cuda/include"
 
 
@@ -27,7 +30,7 @@ def _compile(src: Path, out: Path, extra=()):
     return out
 
 
-@pytest.mark.skipif(not REF_MAIN.exists(), reason="reference checkout not present")
+@pytest.mark.skipif(REF_MAIN is None or not REF_MAIN.exists(), reason="reference checkout not present")
 @pytest.mark.parametrize("profile", [False, True])
 def test_reference_main_compiles_unmodified(tmp_path, built, profile):
     extra = ["-DENABLE_SIM_PROFILE"] if profile else []

@@ -238,12 +238,10 @@ __device__ __forceinline__ void copyOutG(uint32_t *__restrict__ dst, uint32_t sr
 // multiplexer (kind 1: a ? b : c, kind 2: a ? c : b) starts from the pass-c
 // (pass-b) row and blends in the other operand where the select nibble is 1;
 // a word with a select nibble above 1 reads the table window instead.
-template <int SPW, int H>
-__device__ __forceinline__ void fastTop(uint32_t tab, uint32_t lut, const uint32_t (&A)[H], const uint32_t (&B)[H],
-                                        const uint32_t (&C)[H], uint32_t (&v)[H], bool anySel) {
-  const bool isFast = (lut & kFastOp) != 0;
-  const uint32_t kind = isFast ? (lut >> kFastKindShift) & 3u : 0u;
-  const uint32_t g = !isFast ? kGPassC : kind == 0u ? (lut & 15u) : kind == 1u ? kGPassC : kGPassB;
+template <int H>
+__device__ __forceinline__ void fastTop(uint32_t tab, uint32_t lut, uint32_t kind, uint32_t g, const uint32_t (&A)[H],
+                                        const uint32_t (&B)[H], const uint32_t (&C)[H], uint32_t (&v)[H], bool anySel) {
+  g = kind == 0u ? g : kind == 1u ? kGPassC : kGPassB;
   const uint32_t g00 = 0u - (g & 1u), g01 = 0u - ((g >> 1) & 1u), g10 = 0u - ((g >> 2) & 1u), g11 = 0u - (g >> 3);
   const uint32_t k1 = g11 ^ g01, k0 = g10 ^ g00;
 #pragma unroll
@@ -252,16 +250,14 @@ __device__ __forceinline__ void fastTop(uint32_t tab, uint32_t lut, const uint32
     v[i] = Q ^ (C[i] & (P ^ Q));
   }
   if (anySel && kind != 0u) {
-    // select nibbles: 0 or 1 in every stream of the word (SPW = 1: nibble 0)
-    constexpr uint32_t kHigh = SPW == 8 ? 0xEEEEEEEEu : 0xEu;
 #pragma unroll
     for (int i = 0; i < H; ++i) {
-      if ((A[i] & kHigh) == 0u) {
+      if ((A[i] & 0xEEEEEEEEu) == 0u) {  // every select nibble of the word is 0 or 1
         const uint32_t m = (A[i] & 0x11111111u) * 15u;
         const uint32_t X = kind == 1u ? B[i] : C[i];
         v[i] ^= m & (X ^ v[i]);
       } else {
-        v[i] = lookup<SPW>(tab, lut & 0x1FFFu, A[i], B[i], C[i]);
+        v[i] = lookup<8>(tab, lut, A[i], B[i], C[i]);
       }
     }
   }
@@ -279,10 +275,23 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
   // top level: operands < 16 are immediates, else value-pool slots
   if (lane < W) {
     const uint2 t = top.pair(2u * lane);
-    const uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16, b = t.y & 0xFFFFu, c = t.y >> 16;
+    uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16;
+    const uint32_t b = t.y & 0xFFFFu, c = t.y >> 16;
+    // word-wide record (uniform per record): the fast form for 8 streams
+    // per word, the table form (lutIndex, op0) otherwise
+    const bool fastRec = (hdr & kMPFastTop) != 0u;
+    uint32_t kind = 0, fg = 0;
+    if (fastRec) {
+      kind = (lut >> kFastKindShift) & 3u;
+      lut &= 0x1FFFu;
+      if (kind == 0u) {
+        fg = (a >> 4) & 15u;
+        a &= 15u;
+      }
+    }
     uint32_t A[H], B[H], C[H];
     // a word-wide record without multiplexers never reads op0
-    const bool needA = (hdr & (kMPFastTop | kMPFastSel)) != kMPFastTop;
+    const bool needA = !(SPW == 8 && fastRec && !(hdr & kMPFastSel));
     if (constSlots) {
       if (needA) loadG<H>(vpAddr<G>(vp, a, h0), A);
       else {
@@ -311,8 +320,8 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
         loadG<H>(vpAddr<G>(vp, c, h0), C);
       }
     }
-    if (hdr & kMPFastTop) {
-      fastTop<SPW, H>(tab, lut, A, B, C, v, (hdr & kMPFastSel) != 0);
+    if (SPW == 8 && fastRec) {
+      fastTop<H>(tab, lut, kind, fg, A, B, C, v, (hdr & kMPFastSel) != 0);
     } else {
 #pragma unroll
       for (int g = 0; g < H; ++g) v[g] = lut ? lookup<SPW>(tab, lut, A[g], B[g], C[g]) : C[g];

@@ -39,14 +39,15 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 constexpr uint32_t kMPHeaderWords = 4;
 constexpr uint32_t kMPDirectWB = 1u << 30;
 constexpr uint32_t kMPFastTop = 1u << 31, kMPFastSel = 1u << 23;
-// Top-level lut field of a word-wide ("fast") op, in a record with kMPFastTop:
-//   kFastOp | kind << kFastKindShift | payload
-//   kind 0: out = g(b, c) bit by bit, payload = g (bit (x << 1 | y) = g(b bit
-//           x, c bit y));  kind 1: out = a ? b : c;  kind 2: out = a ? c : b
-//   (kinds 1 and 2 for select nibbles 0 and 1; payload = lutIndex, the table
-//   window a word with another select value reads).
-// A lut field without kFastOp in such a record is a move or an idle lane
-// (out = c).
+// Top-level words of a word-wide ("fast") op, in a record with kMPFastTop:
+//   lut field: lutIndex | kind << kFastKindShift | kFastOp
+//   kind 0: out = g(b, c) bit by bit (bit (x << 1 | y) of g = g(b bit x,
+//           c bit y)); op0 field = op0 (an immediate) | g << 4
+//   kind 1: out = a ? b : c, kind 2: out = a ? c : b, for select nibbles 0
+//           and 1 (a word with another select value reads the table)
+// so the table form (lutIndex, op0 & 15 for kind 0) stays available: single
+// streams (one stream per word) evaluate every op by lookup.  A move is kind
+// 0 with g = kGPassC; idle lanes have zero words (g = 0, out = 0).
 constexpr uint32_t kFastOp = 0x8000u, kFastKindShift = 13;
 constexpr uint32_t kGPassC = 0xAu, kGPassB = 0xCu;  // g of "c" and of "b"
 constexpr uint32_t kVecReadWords = 5, kVecOpWords = 3, kMemReadWords = 4;

@@ -103,7 +103,16 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
   for (uint32_t l = 0; l < W; ++l) {
     if (l < m.topLevel.size()) {
       const auto &o = m.topLevel[l];
-      net.push_back(uint32_t(fastTop ? codes[l] : o.lutIndex) | (uint32_t(o.op0) << 16));
+      uint32_t lutW = o.lutIndex, aW = o.op0;
+      if (fastTop) {
+        // the table form stays readable (single streams evaluate by lookups):
+        // lutIndex in bits 0..12, and for kind 0 op0 in bits 0..3 of the op0
+        // field with g above it (a move's op0 is never read)
+        const uint32_t kind = (codes[l] >> kFastKindShift) & 3u;
+        lutW = o.lutIndex | kFastOp | (kind << kFastKindShift);
+        if (kind == 0) aW = (o.lutIndex ? o.op0 & 15u : 0u) | ((codes[l] & 15u) << 4);
+      }
+      net.push_back(lutW | (aW << 16));
       f.fastOps += fastTop && o.lutIndex != 0;
       net.push_back(uint32_t(o.op1) | (uint32_t(o.op2) << 16));
       f.ops += 1;
@@ -132,6 +141,7 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
       net.push_back(0);
   }
   f.kind = kMPLut;
+  f.fastTop = fastTop ? 1u : 0u;
   f.lanes = W;
   f.depth = nMid + 1;
   f.writes = uint32_t(m.lastLevel.size());

@@ -25,6 +25,7 @@ struct MPartFeat {
   uint32_t fanOut = 0;      // later readers of its outputs
   uint32_t partLevels = 0;  // exec levels of its partition
   uint32_t fastOps = 0;     // LUT ops evaluated with word-wide logic (no table read)
+  uint32_t fastTop = 0;     // 1: the top level is word-wide (kMPFastTop)
 };
 
 struct MPartRef {

@@ -64,7 +64,7 @@ float corr(const std::vector<float> &a, const std::vector<float> &b) {
 // 16 structural features of a micro-partition, log-scaled counts.
 void featureVector(const MPartFeat &f, float *x) {
   auto l = [](double v) { return float(std::log1p(v)); };
-  x[0] = f.kind == kMPLut;
+  x[0] = l(f.fastOps);  // LUT ops computed word-wide (kind LUT: x[1..3] all zero)
   x[1] = f.kind == kMPVecRead;
   x[2] = f.kind == kMPVecOp;
   x[3] = f.kind == kMPMemRead;

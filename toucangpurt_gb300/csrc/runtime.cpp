@@ -235,17 +235,20 @@ void fillParams(tgs_sim *h) {
 }
 
 // Launch shape, schedule and per-stream state for the current options.
-// Default warps per block: the most common number of units in an exec level
-// (a LUT micro-partition is one unit, a special one G units), within 6..16,
-// so that a typical level keeps every warp of the block busy (below 6 the
-// wider levels of a design wait on too few warps: on the mixed 4M-LUT design
-// 4 warps ran 236K and 6 warps 247K stimulus-cycles/s).
-uint32_t autoWarps(const DeviceImage &img, uint32_t G) {
+// Default warps per block: the most common amount of work in an exec level,
+// counted in units (a LUT micro-partition is one unit, a special one G units;
+// with 8 streams per word a word-wide LUT micro-partition counts a quarter:
+// three bitwise instructions per word instead of eight table reads), within
+// 6..16, so that a typical level keeps every warp of the block busy (below 6
+// the wider levels of a design wait on too few warps: on the mixed 4M-LUT
+// design 4 warps ran 236K and 6 warps 247K stimulus-cycles/s).
+uint32_t autoWarps(const DeviceImage &img, uint32_t G, uint32_t spw) {
   std::vector<uint64_t> count(33, 0);
   for (const auto &part : img.mp)
     for (const auto &lv : part) {
-      uint32_t u = 0;
-      for (const auto &m : lv) u += m.feat.kind == kMPLut ? 1u : G;
+      uint32_t quarters = 0;
+      for (const auto &m : lv) quarters += m.feat.kind != kMPLut ? 4u * G : (spw == 8 && m.feat.fastTop) ? 1u : 4u;
+      const uint32_t u = (quarters + 3) / 4;
       if (u) count[std::min<uint32_t>(u, 32)]++;
     }
   uint32_t best = 8;
@@ -280,7 +283,7 @@ void configure(tgs_sim *h) {
     while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
   }
   h->gpad = (h->groups + G - 1) / G * G;
-  uint32_t NW = o.warps_per_block ? o.warps_per_block : autoWarps(h->img, uint32_t(G));
+  uint32_t NW = o.warps_per_block ? o.warps_per_block : autoWarps(h->img, uint32_t(G), h->spw);
   if (NW < 1 || NW > 32) throw Error(TGS_ERR_ARG, "warps_per_block must be 1 to 32");
   h->lc.spw = int(h->spw);
   h->lc.G = G;
