@@ -82,7 +82,8 @@ typedef struct tgs_options {
                                 XOR, ...) or a 0/1-select multiplexer -- checked entry by entry against the design's
                                 table at load time -- are computed with word-wide logic for 8 streams at once, and
                                 the ops of single-level LUT micro-partitions of an exec level are regrouped so that
-                                such ops share warps; 1: every op by table lookup.  Takes effect at the next tgs_init */
+                                such ops share warps; 1: every op by table lookup.  Takes effect at the next tgs_init,
+                                for more than one stream (n_streams at init; one stream evaluates by lookup) */
   uint32_t reserved[3];
 } tgs_options;
 

@@ -61,6 +61,10 @@ OPS = [
      (0, 0, 9, IN + 4)],
 ]
 FAST = 8  # LUT ops with a word-wide form (every op but NEAR, ROWSEL with a = 0, RAND and the move)
+# 29 more table ops into unobserved slots: 32 table ops in all, so the 9
+# word-wide ops (the move included) form their own micro-partition (a partial
+# one that fits in the table ops' last micro-partition joins them instead)
+FILL = [(RAND, 0, IN + (i % 16), IN + ((5 * i) % 16)) for i in range(29)]
 
 
 def fast_design() -> dl.Design:
@@ -69,6 +73,7 @@ def fast_design() -> dl.Design:
         lanes = [dl.top(*op) for op in mp]
         level.append(dl.MPart(top=lanes, wbs=[dl.wb(32 + i, OUT + k + i) for i in range(len(mp))]))
         k += len(mp)
+    level.append(dl.MPart(top=[dl.top(*op) for op in FILL], wbs=[dl.wb(32 + i, 100 + i) for i in range(len(FILL))]))
     return frame([level], lut=fast_table())
 
 
@@ -100,10 +105,10 @@ def test_palette_rows_recognised(tmp_path, built):
     dp = tmp_path / "fast.bin"
     fast_design().write(dp)
     st = repack(dp, tmp_path / "r.bin")
-    assert st.lut_ops == 11 and st.fast_lut_ops == FAST
+    assert st.lut_ops == 11 + len(FILL) and st.fast_lut_ops == FAST
     # the ops are regrouped: word-wide ops (bitwise, then multiplexers) share
-    # micro-partitions, table ops the others
-    assert st.mparts_after == st.mparts_before - 1
+    # one micro-partition, the 32 table ops another
+    assert (st.mparts_before, st.mparts_after, st.fast_mparts) == (5, 3, 1)
     off = repack(dp, tmp_path / "n.bin", lane_packing=0, fast=0)
     assert off.fast_lut_ops == 0 and off.mparts_after == off.mparts_before
 
@@ -205,3 +210,19 @@ def test_palette_designs_gpu(palette, name, fast):
     np.testing.assert_array_equal(got.cycle_digest, ref["cycle_digest"])
     for k in ("final_reg_digest", "final_mem_digest", "rolling_digest"):
         np.testing.assert_array_equal(getattr(got, k), ref[k], err_msg=k)
+
+
+def test_partial_wordwide_group_joins_table_ops(tmp_path, built):
+    """A level of 9 word-wide and 3 table ops: the word-wide group would be a
+    second warp pass, so its ops stay with the table ops (one micro-partition,
+    evaluated by lookup) -- and still compute the same values."""
+    d = fast_design()
+    d.parts[0].levels[1] = d.parts[0].levels[1][:3]  # without the filler ops
+    dp = tmp_path / "f.bin"
+    d.write(dp)
+    st = repack(dp, tmp_path / "r.bin")
+    assert (st.mparts_before, st.mparts_after, st.fast_mparts, st.fast_lut_ops) == (4, 2, 0, 0)
+    s = pyoracle.OracleState(pyoracle.OracleDesign(tmp_path / "r.bin"))
+    s.regs()[:16] = inputs(3)
+    s.eval(1)
+    np.testing.assert_array_equal(s.regs()[16:48], expected(3))

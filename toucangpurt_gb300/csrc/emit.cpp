@@ -318,6 +318,14 @@ std::vector<CGMicroPartInfo> regroupLevel(const std::vector<CGMicroPartInfo> &in
   for (const Item &it : items)
     if (it.results.size() > 32) return in;  // more write-back entries than one micro-partition holds
   std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.cls < b.cls; });
+  // a partial word-wide micro-partition that would add a warp pass to the
+  // level (its ops fit in the partial table one) joins the table ops instead
+  {
+    const size_t F = size_t(std::count_if(items.begin(), items.end(), [](const Item &it) { return it.cls < 2; }));
+    const size_t T = items.size() - F;
+    if (F % 32 && T % 32 && F % 32 + T % 32 <= 32)
+      for (size_t i = F - F % 32; i < F; ++i) items[i].cls = 2;
+  }
   std::vector<CGMicroPartInfo> out;
   for (uint32_t i = 0; i < in.size(); ++i)
     if (!(in[i].isLUTPart && in[i].middleLevels.empty() && !in[i].lastLevel.empty())) out.push_back(in[i]);

@@ -518,7 +518,7 @@ void upload(tgs_sim *h) {
   cudaStream_t s = h->stream;
   buildProbes(h);
   buildImage(h->design, h->img, h->opt.value_pool == 0, h->captureSignals ? &h->probes : nullptr,
-             h->opt.lane_packing == 0, h->opt.fast_luts == 0);
+             h->opt.lane_packing == 0, h->opt.fast_luts == 0 && h->opt.n_streams > 1);
   h->net.upload(h->img.net, s);
   h->constVec.upload(h->img.constVec, s);
   std::vector<uint8_t> lut(kLutTablePadded, 0);
