@@ -443,7 +443,8 @@ typedef struct tgs_repack_stats {
   uint64_t lut_ops;        /* LUT ops with lutIndex != 0 */
   uint64_t fast_lut_ops;   /* of which evaluated with word-wide logic */
   uint64_t fast_mparts;    /* micro-partitions whose top level is word-wide */
-  uint64_t reserved[3];
+  uint64_t exec_levels;    /* exec levels of all partitions */
+  uint64_t reserved[2];
 } tgs_repack_stats;
 int tgs_repack_design(const char *in_path, const char *out_path, int lane_packing, int fast_luts,
                       tgs_repack_stats *stats);

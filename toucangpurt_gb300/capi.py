@@ -128,7 +128,8 @@ MLP_PARAMS = 5313
 # except tgs_last_error / tgs_version.
 class RepackStats(C.Structure):
     _fields_ = [("mparts_before", C.c_uint64), ("mparts_after", C.c_uint64), ("lut_ops", C.c_uint64),
-                ("fast_lut_ops", C.c_uint64), ("fast_mparts", C.c_uint64), ("reserved", C.c_uint64 * 3)]
+                ("fast_lut_ops", C.c_uint64), ("fast_mparts", C.c_uint64), ("exec_levels", C.c_uint64),
+                ("reserved", C.c_uint64 * 2)]
 
 
 SIGNATURES = {

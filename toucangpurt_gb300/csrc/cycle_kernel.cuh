@@ -424,6 +424,12 @@ __device__ __forceinline__ void evalVecRead(const KParams &p, const PartDesc &d,
 // Work item = (op, group, stream), one per lane: the SPW lanes of one (op,
 // group) hold the streams of one word and merge their result nibbles with
 // shuffles, so no lane runs the streams of a word one after another.
+// Vectors of up to 16 nibbles (the usual 32- and 64-bit ones) compute in
+// 64-bit registers: after sign extension to 64 bits every value lies in
+// [-2^63, 2^63), so the comparisons equal the reference's 128-bit ones, and
+// sums, differences and products agree with them in the low 64 bits, which
+// hold every result nibble (i < len <= 16).  Longer vectors take 128-bit
+// arithmetic as the reference does.
 template <int SPW, int G, bool SH>
 __device__ void evalVecOp(const KParams &p, const PartDesc &d, const Words<SH> mp, uint32_t hdr, uint32_t vp,
                           uint32_t lane, uint32_t g0, uint32_t gn) {
@@ -442,15 +448,41 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const Words<SH> m
     const uint32_t cf = w1 >> 24;
     const bool c1 = (cf & 2u) != 0, c2 = (cf & 1u) != 0;
     const bool isVec = opc <= 2;
-    unsigned __int128 a = 0, b = 0;
-    for (uint32_t i = 0; i < len; ++i) {
-      const uint32_t x = c1 ? (uint32_t(__ldg(cv + v1 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v1 + i, g)), k);
-      const uint32_t y = c2 ? (uint32_t(__ldg(cv + v2 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v2 + i, g)), k);
-      a |= (unsigned __int128)x << (4 * i);
-      b |= (unsigned __int128)y << (4 * i);
-    }
+    const bool narrow = len <= 16u;
+    auto nibA = [&](uint32_t i) {
+      return c1 ? (uint32_t(__ldg(cv + v1 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v1 + i, g)), k);
+    };
+    auto nibB = [&](uint32_t i) {
+      return c2 ? (uint32_t(__ldg(cv + v2 + i)) & 15u) : nib(ldsU32(vpAddr<G>(vp, v2 + i, g)), k);
+    };
+    unsigned long long r64 = 0;
     unsigned __int128 rv = 0;
-    if (act) {
+    if (narrow) {
+      unsigned long long a = 0, b = 0;
+#pragma unroll 4
+      for (uint32_t i = 0; i < len; ++i) {
+        a |= (unsigned long long)nibA(i) << (4 * i);
+        b |= (unsigned long long)nibB(i) << (4 * i);
+      }
+      if (len) {
+        const uint32_t s = 64u - 4u * len;  // sign extension from bit 4 * len - 1
+        const long long sa = (long long)(a << s) >> s, sb = (long long)(b << s) >> s;
+        switch (opc) {
+          case 0: r64 = (unsigned long long)sa + (unsigned long long)sb; break;
+          case 1: r64 = (unsigned long long)sa - (unsigned long long)sb; break;
+          case 2: r64 = (unsigned long long)sa * (unsigned long long)sb; break;
+          case 3: r64 = sa == sb; break;
+          case 4: r64 = sa < sb; break;
+          case 5: r64 = sa <= sb; break;
+          default: r64 = 0; break;
+        }
+      }
+    } else {
+      unsigned __int128 a = 0, b = 0;
+      for (uint32_t i = 0; i < len; ++i) {
+        a |= (unsigned __int128)nibA(i) << (4 * i);
+        b |= (unsigned __int128)nibB(i) << (4 * i);
+      }
       const uint32_t sign = 4 * len - 1;
       if ((a >> sign) & 1) a |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
       if ((b >> sign) & 1) b |= ~(((unsigned __int128)1 << (sign + 1)) - 1);
@@ -471,7 +503,8 @@ __device__ void evalVecOp(const KParams &p, const PartDesc &d, const Words<SH> m
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) maxLen = max(maxLen, __shfl_xor_sync(kFull, maxLen, o));
     for (uint32_t i = 0; i < maxLen; ++i) {
-      uint32_t word = i < outLen ? (uint32_t(rv >> (4 * i)) & 15u) << (4 * k) : 0u;
+      const uint32_t x = narrow ? uint32_t(r64 >> (4 * (i & 15u))) : uint32_t(rv >> (4 * i));
+      uint32_t word = i < outLen ? (x & 15u) << (4 * k) : 0u;
 #pragma unroll
       for (int o = 1; o < SPW; o <<= 1) word |= __shfl_xor_sync(kFull, word, o);
       if (k == 0 && i < outLen) stsU32(vpAddr<G>(vp, (res + i) & 0xFFFFu, g), word);

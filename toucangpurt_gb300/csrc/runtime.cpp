@@ -1922,6 +1922,7 @@ extern "C" int tgs_repack_design(const char *in, const char *out, int lanePackin
     FastLuts *fast = fastLuts && d.lut.size() == kLutSize ? &fl : nullptr;
     for (auto &p : d.parts)
       for (auto &lvl : p.exec_mParts) {
+        st.exec_levels += 1;
         st.mparts_before += lvl.size();
         if (lanePacking) lvl = packLevel(lvl);
         if (fast) lvl = regroupLevel(lvl, fast);
