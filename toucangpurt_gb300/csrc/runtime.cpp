@@ -328,8 +328,28 @@ void configure(tgs_sim *h) {
                                        " B of shared memory; lower groups_per_item");
   // first pass to learn the largest level block (independent of the block count)
   buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, 1, nGB, h->sched);
+  // Stage buffer size: the largest level, or a smaller size that still
+  // stages nearly every level when it puts more blocks on an SM (levels
+  // larger than the buffers are read from global memory; mixed 4M-LUT
+  // design: 4 -> 5 blocks per SM, 256K -> 310K stimulus-cycles/s)
   uint32_t stage = o.resident_netlist == 2 ? 0u : std::min<uint32_t>(h->sched.maxLevelWords, 4096u);
   int perSM = shape(stage);
+  if (stage) {
+    std::vector<uint32_t> sizes;
+    for (size_t i = 1; i < h->sched.levelDesc.size(); i += 2) sizes.push_back(h->sched.levelDesc[i]);
+    std::sort(sizes.begin(), sizes.end());
+    // items in flight: blocks on the GPU at once, up to the items of a region
+    auto inFlight = [&](int n) { return std::min(maxItems, size_t(std::max(n, 0)) * size_t(h->props.multiProcessorCount)); };
+    for (double q : {0.99, 0.98, 0.95}) {
+      const uint32_t cand = (sizes[size_t(q * double(sizes.size() - 1))] + 3u) & ~3u;
+      if (cand >= stage || cand == 0) continue;
+      const int n = shape(cand);
+      if (inFlight(n) > inFlight(perSM)) {
+        stage = cand;
+        perSM = n;
+      }
+    }
+  }
   const int perSMNoStage = shape(0);
   if (stage && perSM < std::max(1, perSMNoStage / 2)) {  // keep at least half the occupancy
     stage = std::min<uint32_t>(stage, 1024u);
