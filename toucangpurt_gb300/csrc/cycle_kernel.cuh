@@ -272,11 +272,16 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
   const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
   const Words<SH> top = mp.at(kMPHeaderWords);
   uint32_t v[H];
+  uint32_t cres = 0;  // compact records: the lane's write-back slot
   // top level: operands < 16 are immediates, else value-pool slots
   if (lane < W) {
     const uint2 t = top.pair(2u * lane);
-    uint32_t lut = t.x & 0xFFFFu, a = t.x >> 16;
-    const uint32_t b = t.y & 0xFFFFu, c = t.y >> 16;
+    // compact lanes (uniform per record) carry the write-back slot
+    const bool compact = (hdr & kMPCompact) != 0u;
+    uint32_t lut = compact ? t.y >> 16 : t.x & 0xFFFFu, a = compact ? t.x & 0xFFFu : t.x >> 16;
+    const uint32_t b = compact ? (t.x >> 12) & 0xFFFu : t.y & 0xFFFFu;
+    const uint32_t c = compact ? (t.x >> 24) | ((t.y & 15u) << 8) : t.y >> 16;
+    cres = (t.y >> 4) & 0xFFFu;
     // word-wide record (uniform per record): the fast form for 8 streams
     // per word, the table form (lutIndex, op0) otherwise
     const bool fastRec = (hdr & kMPFastTop) != 0u;
@@ -354,7 +359,11 @@ __device__ __forceinline__ void evalLutPass(const Words<SH> mp, uint32_t hdr, ui
     for (int g = 0; g < H; ++g) v[g] = nv[g];
   }
   // write-back (SimEval.cu:422-447): shuffleId < 32 immediate, else lane
-  // (shuffleId mod 32)
+  // (shuffleId mod 32); a compact record's lane l writes its own value
+  if (hdr & kMPCompact) {
+    if (lane < nWB) storeG<H>(vpAddr<G>(vp, cres, h0), v);
+    return;
+  }
   const Words<SH> wb = mid.at(nMid * W);
   const uint32_t wv = lane < nWB ? wb[lane] : 0u;
   const uint32_t src = wv & 0xFFu, res = wv >> 16;

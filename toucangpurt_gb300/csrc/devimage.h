@@ -26,11 +26,14 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 // shuffleId == 32 + l for every entry, so no lane exchange is needed)
 // | fast top level << 31 (every top-level op has a word-wide form: its lut
 // field holds the fast code of emit.h, not a table offset) | some fast op is
-// a multiplexer << 23.
+// a multiplexer << 23 | compact lanes << 22 (see below).
 // LUT micro-partition words after the 4-word header (all lane-major):
 //   top:  2 * W words, lane l: [lutIndex | op0 << 16, op1 | op2 << 16] (zero for idle lanes)
 //   mid:  nMid * W words, the reference's packed middle-level op (zero = move of immediate 0)
 //   wb :  W words, lane l: shuffleId | result << 16
+// A compact record (no middle levels, write-back entry l = lane l for every
+// lane, all slots below 4096) holds one word pair per lane and no wb block:
+//   lane l: [op0 | op1 << 12 | (op2 & 255) << 24, op2 >> 8 | result << 4 | lut field << 16]
 // Special micro-partitions: header, then per lane fixed-size records:
 //   VecRead (5 words): vecBase | vecLength << 16, offset | isConst << 16,
 //                      idx0 | idx1 << 16, idx2 | idx3 << 16, outRange | result << 16
@@ -38,7 +41,7 @@ enum : uint32_t { kMPLut = 0, kMPVecRead = 1, kMPVecOp = 2, kMPMemRead = 3 };
 //   MemRead (4 words): memBase lo, memBase hi | multiWriter << 31, en | addrVec << 16, result
 constexpr uint32_t kMPHeaderWords = 4;
 constexpr uint32_t kMPDirectWB = 1u << 30;
-constexpr uint32_t kMPFastTop = 1u << 31, kMPFastSel = 1u << 23;
+constexpr uint32_t kMPFastTop = 1u << 31, kMPFastSel = 1u << 23, kMPCompact = 1u << 22;
 // Top-level words of a word-wide ("fast") op, in a record with kMPFastTop:
 //   lut field: lutIndex | kind << kFastKindShift | kFastOp
 //   kind 0: out = g(b, c) bit by bit (bit (x << 1 | y) of g = g(b bit x,

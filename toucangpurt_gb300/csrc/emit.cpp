@@ -92,11 +92,19 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
     fastTop = codes.back() != 0;
     sel = sel || ((codes.back() >> kFastKindShift) & 3u) != 0;
   }
+  // compact lanes (one word pair per op, the write-back slot inside it): a
+  // single-level record whose entry l writes lane l's value, with every slot
+  // below 4096 (renumbered value pools are far smaller)
+  bool compact = nMid == 0 && direct && !m.topLevel.empty() && m.lastLevel.size() == m.topLevel.size();
+  for (size_t l = 0; compact && l < m.topLevel.size(); ++l) {
+    const auto &o = m.topLevel[l];
+    compact = o.op0 < 4096 && o.op1 < 4096 && o.op2 < 4096 && m.lastLevel[l].result < 4096;
+  }
   align4(net);
   uint32_t off = uint32_t(net.size());
   net.push_back(kMPLut | (W << 2) | (nMid << 8) | (uint32_t(m.lastLevel.size()) << 16) |
                 (uint32_t(m.topLevel.size()) << 24) | (direct ? kMPDirectWB : 0u) | (fastTop ? kMPFastTop : 0u) |
-                (fastTop && sel ? kMPFastSel : 0u));
+                (fastTop && sel ? kMPFastSel : 0u) | (compact ? kMPCompact : 0u));
   net.push_back(0);
   net.push_back(0);
   net.push_back(0);
@@ -112,9 +120,15 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
         lutW = o.lutIndex | kFastOp | (kind << kFastKindShift);
         if (kind == 0) aW = (o.lutIndex ? o.op0 & 15u : 0u) | ((codes[l] & 15u) << 4);
       }
-      net.push_back(lutW | (aW << 16));
+      if (compact) {
+        const uint32_t c = o.op2, res = m.lastLevel[l].result;
+        net.push_back(aW | (uint32_t(o.op1) << 12) | ((c & 0xFFu) << 24));
+        net.push_back((c >> 8) | (res << 4) | (lutW << 16));
+      } else {
+        net.push_back(lutW | (aW << 16));
+        net.push_back(uint32_t(o.op1) | (uint32_t(o.op2) << 16));
+      }
       f.fastOps += fastTop && o.lutIndex != 0;
-      net.push_back(uint32_t(o.op1) | (uint32_t(o.op2) << 16));
       f.ops += 1;
       f.nops += o.lutIndex == 0;
       f.vpReads += (o.op0 >= 16) + (o.op1 >= 16) + (o.op2 >= 16);
@@ -134,7 +148,7 @@ uint32_t emitLut(const CGMicroPartInfo &m, std::vector<uint32_t> &net, MPartFeat
         f.threeOp += ((w >> 12) & 63) >= 32;
       }
     }
-  for (uint32_t l = 0; l < W; ++l) {
+  for (uint32_t l = 0; l < W && !compact; ++l) {
     if (l < m.lastLevel.size())
       net.push_back(uint32_t(m.lastLevel[l].shuffleId) | (uint32_t(m.lastLevel[l].result) << 16));
     else
