@@ -317,7 +317,8 @@ def make_simulator(a, dp, sp, streams, gpu):
         notes["options"] = list(a.set)
     if a.autotune:
         best, trials = s.autotune(cycles=8, warmup=2)
-        notes["autotuned"] = {k: best[k] for k in ("groups_per_item", "warps_per_block", "blocks_per_sm", "mode", "staged")}
+        notes["autotuned"] = {k: best[k] for k in ("groups_per_item", "warps_per_block", "blocks_per_sm", "mode", "staged",
+                                                   "mpart_lanes", "levels_per_barrier")}
         notes["autotune_trials"] = len(trials)
     return s, notes
 

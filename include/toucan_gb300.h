@@ -84,7 +84,14 @@ typedef struct tgs_options {
                                 the ops of single-level LUT micro-partitions of an exec level are regrouped so that
                                 such ops share warps; 1: every op by table lookup.  Takes effect at the next tgs_init,
                                 for more than one stream (n_streams at init; one stream evaluates by lookup) */
-  uint32_t reserved[3];
+  uint32_t mpart_lanes;      /* micro-partition size: LUTs a warp takes at once from an exec level's plan, 32
+                                (0, the default), 64 or 128 -- 32-lane micro-partitions bundled by two or four when
+                                warps are handed their share of a level (fewer, larger units per warp) */
+  uint32_t levels_per_barrier; /* 1 (0, the default), 2 or 4: consecutive exec levels of a partition may run as one
+                                block without a block barrier between them where every dependency among their
+                                micro-partitions stays on one warp and the merged block is scheduled no longer than
+                                the levels apart (chains of narrow cones); values are unchanged */
+  uint32_t reserved[1];
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u
@@ -96,9 +103,10 @@ int tgs_default_options(tgs_options *opt);
 
 /* Autotuner (no counterpart in the reference): times short runs of the loaded
  * design at the handle's stream count over groups_per_item x warps_per_block {4, 6, 8, 12, 16}
- * x blocks_per_sm x mode (x staging), keeps the fastest as the handle's
- * options and resets the state to the initial state.  Micro-partition sizes
- * are fixed by the design file; these are the launch-side knobs. */
+ * x blocks_per_sm x mode (x staging), then, with the fastest of those, over
+ * micro-partition size (mpart_lanes {32, 64, 128}) x levels per barrier
+ * {1, 2, 4}; keeps the fastest as the handle's options and resets the state
+ * to the initial state. */
 typedef struct tgs_tune_opts {
   uint32_t cycles;       /* timed cycles per trial (0 = 16) */
   uint32_t warmup;       /* untimed cycles per trial (0 = 2) */
@@ -112,6 +120,7 @@ typedef struct tgs_tune_trial {
   uint32_t staged;      /* exec levels: 1 staged per level, 2 resident for the launch, 0 read from global memory */
   uint32_t blocks;      /* grid size of the trial */
   float ms_per_cycle;   /* negative: the configuration does not fit */
+  uint32_t mpart_lanes, levels_per_barrier;
 } tgs_tune_trial;
 
 /* trials (optional, max_trials entries) receives every trial; best receives the winner */
@@ -316,7 +325,8 @@ typedef struct tgs_design_stats {
   uint32_t smem_per_block;   /* dynamic shared memory of a block: table, stage buffers, value pool */
   uint32_t stage_words;      /* words of one exec-level stage buffer (0: levels resident or read from global memory) */
   uint32_t resident_words;   /* words of a block's resident exec levels (0: staged or read from global memory) */
-  uint32_t reserved[5];
+  uint32_t fused_levels;     /* exec levels merged into the block before them (levels_per_barrier > 1) */
+  uint32_t reserved[4];
 } tgs_design_stats;
 int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *out);
 

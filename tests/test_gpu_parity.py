@@ -3,6 +3,8 @@
 Bit-exact equality on the same seeded inputs: per-cycle register digests,
 rolling digests, final register/memory digests, full final state, stop cycles.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -276,3 +278,41 @@ def test_copy_profile_data(designs, name):
         assert (useful > 0).all() and (useful <= total).all(), (useful[:8], total[:8])
         st.eval(230)
         np.testing.assert_array_equal(s.reg_pool(), st.regs())
+
+
+def _design_levels(dp) -> int:
+    import ctypes as C
+    import tempfile
+
+    st = sim.capi.RepackStats()
+    with tempfile.TemporaryDirectory() as td:
+        sim.capi.check(sim.capi.lib().tgs_repack_design(str(dp).encode(), str(Path(td) / "r.bin").encode(), 0, 0,
+                                                        C.byref(st)))
+    return st.exec_levels
+
+
+@pytest.mark.parametrize("name", ["mixed", "deep_cones", "wide3op", "small"])
+@pytest.mark.parametrize("lanes", [32, 64, 128])
+@pytest.mark.parametrize("lpb", [1, 2, 4])
+def test_schedule_knobs(designs, name, lanes, lpb):
+    """Micro-partition size (LUTs a warp takes at once: 32, 64, 128) and
+    levels per barrier (1, 2, 4 exec levels merged into one block where every
+    dependency stays on one warp) only move the schedule: bit-exact results
+    for batched streams (resident and staged levels, both forms) and a single
+    stream."""
+    dp, sp, info = designs[name]
+    stim = _stim(info, seed=23)
+    ref = None
+    for streams, levels, mode in ((24, 0, 0), (24, 3, 1), (1, 0, 0)):
+        cyc = np.full(streams, 24, np.uint32)
+        with sim.Simulator(n_streams=streams, groups_per_item=2 if streams > 1 else 0, resident_netlist=levels,
+                           mode=mode, mpart_lanes=lanes, levels_per_barrier=lpb) as s:
+            s.init(0, dp, sp, False, False)
+            st = s.design_stats()
+            # every exec level of the design is a block of its own or merged into one
+            assert st["exec_levels"] + st["fused_levels"] == _design_levels(dp)
+            if lpb == 1:
+                assert st["fused_levels"] == 0
+            got = s.batch_run(cyc, stim, cycle_digests=True)
+        r = pyoracle.OracleDesign(dp, sp).run(cyc, stim, cycle_digests=True)
+        _compare(got, r)

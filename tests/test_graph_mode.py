@@ -89,9 +89,13 @@ def test_autotune_then_parity(small):
         assert best["ms_per_cycle"] > 0 and len(trials) >= 2
         assert {t["mode"] for t in trials} == {0, 1}
         assert best["ms_per_cycle"] == min(t["ms_per_cycle"] for t in trials if t["ms_per_cycle"] > 0)
+        # the schedule axes: micro-partition size x levels per barrier
+        assert {(t["mpart_lanes"], t["levels_per_barrier"]) for t in trials} == {
+            (a, b) for a in (32, 64, 128) for b in (1, 2, 4)}
         o = s.options()
         assert (o["groups_per_item"], o["warps_per_block"], o["mode"]) == (
             best["groups_per_item"], best["warps_per_block"], best["mode"])
+        assert (o["mpart_lanes"], o["levels_per_barrier"]) == (best["mpart_lanes"], best["levels_per_barrier"])
         got = s.batch_run(cyc, stim, cycle_digests=True)
     ref = pyoracle.OracleDesign(dp, sp).run(cyc, stim, cycle_digests=True)
     np.testing.assert_array_equal(got.cycle_digest, ref["cycle_digest"])

@@ -40,7 +40,8 @@ class Options(C.Structure):
         ("blocks_per_sm", C.c_uint32), ("schedule", C.c_uint32), ("mode", C.c_uint32),
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
         ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("lane_packing", C.c_uint32),
-        ("fast_luts", C.c_uint32), ("reserved", C.c_uint32 * 3),
+        ("fast_luts", C.c_uint32), ("mpart_lanes", C.c_uint32), ("levels_per_barrier", C.c_uint32),
+        ("reserved", C.c_uint32 * 1),
     ]
 
 
@@ -98,7 +99,8 @@ class DesignStats(C.Structure):
         ("max_exec_levels", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
         ("groups_per_item", C.c_uint32), ("streams_per_word", C.c_uint32), ("block_barriers", C.c_uint64),
         ("exec_levels", C.c_uint64), ("makespan", C.c_double * 2), ("smem_per_block", C.c_uint32),
-        ("stage_words", C.c_uint32), ("resident_words", C.c_uint32), ("reserved", C.c_uint32 * 5),
+        ("stage_words", C.c_uint32), ("resident_words", C.c_uint32), ("fused_levels", C.c_uint32),
+        ("reserved", C.c_uint32 * 4),
     ]
 
 
@@ -119,7 +121,8 @@ class TuneOpts(C.Structure):
 
 class TuneTrial(C.Structure):
     _fields_ = [("groups_per_item", C.c_uint32), ("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32),
-                ("mode", C.c_uint32), ("staged", C.c_uint32), ("blocks", C.c_uint32), ("ms_per_cycle", C.c_float)]
+                ("mode", C.c_uint32), ("staged", C.c_uint32), ("blocks", C.c_uint32), ("ms_per_cycle", C.c_float),
+                ("mpart_lanes", C.c_uint32), ("levels_per_barrier", C.c_uint32)]
 
 
 MLP_PARAMS = 5313

@@ -614,60 +614,178 @@ void buildImage(const SimDesignInfo &d, DeviceImage &img, bool compactSlots, con
 // Greedy gate-count cost of a micro-partition (the fallback cost model).
 float gateCost(const MPartFeat &f) { return float(std::max<uint32_t>(1, f.ops)); }
 
+namespace {
+
+// Union-find over micro-partitions (fusing exec levels).
+struct Dsu {
+  std::vector<uint32_t> p;
+  explicit Dsu(size_t n) : p(n) { std::iota(p.begin(), p.end(), 0u); }
+  uint32_t find(uint32_t x) {
+    while (p[x] != x) x = p[x] = p[p[x]];
+    return x;
+  }
+  void join(uint32_t a, uint32_t b) { p[find(a)] = find(b); }
+};
+
+}  // namespace
+
 void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,
                    const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,
-                   Schedule &out) {
+                   Schedule &out, const SchedOpts &so) {
   out = Schedule();
   out.NW = NW;
   out.partCost.assign(d.parts.size(), 0.0);
   auto &sw = out.words;
+  const uint32_t bundle = std::max<uint32_t>(1, so.unitLanes / 32);
+  const uint32_t lpb = std::max<uint32_t>(1, so.levelsPerBarrier);
+  // a unit of work: micro-partition i of exec level lv, stream groups [g0, g0 + gn)
+  struct Unit {
+    uint32_t lv, i, g0, gn;
+    double c;
+  };
+  using Plan = std::vector<std::vector<Unit>>;  // units per warp, in execution order
   for (uint32_t pid = 0; pid < d.parts.size(); ++pid) {
     PartDesc &pd = img.parts[pid];
+    const auto &levels = img.mp[pid];
+    const uint32_t nLv = uint32_t(levels.size());
     pd.schedOff = uint32_t(out.levelDesc.size() / 2);
     double total = 0;
+    auto costOf = [&](uint32_t lv, uint32_t i) {
+      return cost ? double((*cost)[pid][lv][i]) : double(gateCost(levels[lv][i].feat));
+    };
+    // One exec level on its own: a LUT micro-partition runs every group of the
+    // item in one warp (its lanes share the operand loads), a special one is
+    // split into one unit per group (a level holding one of them keeps G warps
+    // busy); LUT units go to warps in bundles of `bundle` (micro-partitions of
+    // 32 x bundle LUTs per warp), largest cost first onto the least loaded warp.
+    auto planLevel = [&](uint32_t lv, Plan &plan) {
+      const auto &mps = levels[lv];
+      std::vector<std::vector<Unit>> items;  // LPT items: bundles of units
+      std::vector<Unit> luts;
+      for (uint32_t i = 0; i < mps.size(); ++i) {
+        if (mps[i].feat.kind != kMPLut && G > 1)
+          for (uint32_t g = 0; g < G; ++g) items.push_back({{lv, i, g, 1, costOf(lv, i) / G}});
+        else
+          luts.push_back({lv, i, 0, G, costOf(lv, i)});
+      }
+      std::stable_sort(luts.begin(), luts.end(), [](const Unit &a, const Unit &b) { return a.c > b.c; });
+      for (size_t k = 0; k < luts.size(); k += bundle)
+        items.emplace_back(luts.begin() + k, luts.begin() + std::min(luts.size(), k + bundle));
+      std::vector<double> ic(items.size(), 0.0);
+      for (size_t k = 0; k < items.size(); ++k)
+        for (auto &u : items[k]) ic[k] += u.c;
+      std::vector<uint32_t> order(items.size());
+      std::iota(order.begin(), order.end(), 0u);
+      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return ic[a] > ic[b]; });
+      std::vector<double> load(NW, 0.0);
+      plan.assign(NW, {});
+      for (uint32_t k : order) {
+        const uint32_t w = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
+        load[w] += ic[k];
+        plan[w].insert(plan[w].end(), items[k].begin(), items[k].end());
+      }
+      return *std::max_element(load.begin(), load.end());
+    };
+    // Exec levels [lv, lv + m) as one block without barriers inside: micro-
+    // partitions that touch a slot one of them writes (across the levels)
+    // form one component, a component runs on one warp level by level, and
+    // components go to warps largest first.  Special micro-partitions run
+    // every group in one unit.
+    auto planFused = [&](uint32_t lv, uint32_t m, Plan &plan) {
+      std::vector<std::pair<uint32_t, uint32_t>> ids;  // (level, i)
+      for (uint32_t l = lv; l < lv + m; ++l)
+        for (uint32_t i = 0; i < levels[l].size(); ++i) ids.push_back({l, i});
+      Dsu dsu(ids.size());
+      std::vector<int32_t> lastW(pd.vpSlots + 64, -1);
+      std::vector<std::vector<uint32_t>> readers(pd.vpSlots + 64);
+      size_t at = 0;
+      for (uint32_t l = lv; l < lv + m; ++l) {
+        const size_t first = at;
+        for (uint32_t i = 0; i < levels[l].size(); ++i, ++at) {
+          const MPartRef &r = levels[l][i];
+          for (uint32_t s : r.reads)
+            if (lastW[s] >= 0) dsu.join(uint32_t(at), uint32_t(lastW[s]));
+          for (uint32_t s : r.writes) {
+            if (lastW[s] >= 0) dsu.join(uint32_t(at), uint32_t(lastW[s]));
+            for (uint32_t x : readers[s]) dsu.join(uint32_t(at), x);
+          }
+        }
+        // the level's own accesses count from the next level on (micro-
+        // partitions of one level touch disjoint slots)
+        for (size_t k = first; k < at; ++k) {
+          const MPartRef &r = levels[ids[k].first][ids[k].second];
+          for (uint32_t s : r.reads) readers[s].push_back(uint32_t(k));
+          for (uint32_t s : r.writes) {
+            lastW[s] = int32_t(k);
+            readers[s].clear();
+          }
+        }
+      }
+      std::vector<double> cc(ids.size(), 0.0);
+      std::vector<std::vector<uint32_t>> members(ids.size());
+      for (size_t k = 0; k < ids.size(); ++k) {
+        const uint32_t root = dsu.find(uint32_t(k));
+        cc[root] += costOf(ids[k].first, ids[k].second);
+        members[root].push_back(uint32_t(k));
+      }
+      std::vector<uint32_t> roots;
+      for (uint32_t k = 0; k < ids.size(); ++k)
+        if (!members[k].empty()) roots.push_back(k);
+      std::stable_sort(roots.begin(), roots.end(), [&](uint32_t a, uint32_t b) { return cc[a] > cc[b]; });
+      std::vector<double> load(NW, 0.0);
+      plan.assign(NW, {});
+      for (uint32_t rt : roots) {
+        const uint32_t w = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
+        load[w] += cc[rt];
+        for (uint32_t k : members[rt])
+          plan[w].push_back({ids[k].first, ids[k].second, 0, G, costOf(ids[k].first, ids[k].second)});
+      }
+      for (auto &wu : plan)
+        std::stable_sort(wu.begin(), wu.end(), [](const Unit &a, const Unit &b) { return a.lv < b.lv; });
+      return *std::max_element(load.begin(), load.end());
+    };
+
     // barrier placement: hazards since the last block barrier, tracked per slot
     std::vector<int32_t> lastWriter(pd.vpSlots + 64, -1);  // warp of last write since the barrier
     std::vector<uint32_t> readersMask(pd.vpSlots + 64, 0);  // warps that read since the barrier
     std::vector<uint32_t> touched;
-    for (uint32_t lv = 0; lv < pd.nLevels; ++lv) {
-      const auto &mps = img.mp[pid][lv];
-      auto costOf = [&](uint32_t i) { return cost ? (*cost)[pid][lv][i] : gateCost(mps[i].feat); };
-      // units: a LUT micro-partition runs every group of the item in one warp
-      // (its lanes share the operand loads); a special one is split into one
-      // unit per group, so a level holding one of them keeps G warps busy
-      struct Unit {
-        uint32_t i, g0, gn;
-        double c;
-      };
-      std::vector<Unit> units;
-      for (uint32_t i = 0; i < mps.size(); ++i) {
-        if (mps[i].feat.kind != kMPLut && G > 1)
-          for (uint32_t g = 0; g < G; ++g) units.push_back({i, g, 1, costOf(i) / G});
-        else
-          units.push_back({i, 0, G, costOf(i)});
+    uint32_t blocks = 0;
+    for (uint32_t lv = 0; lv < nLv;) {
+      Plan plan;
+      double mk = planLevel(lv, plan);
+      uint32_t n = 1;
+      if (lpb > 1) {
+        // fuse as many levels (up to lpb) as run no longer on their warps
+        // than the same levels with a barrier between each
+        std::vector<double> single;
+        for (uint32_t l = lv; l < std::min(nLv, lv + lpb); ++l) {
+          Plan tmp;
+          single.push_back(l == lv ? mk : planLevel(l, tmp));
+        }
+        for (uint32_t m = uint32_t(single.size()); m >= 2; --m) {
+          Plan fused;
+          const double fmk = planFused(lv, m, fused);
+          double sep = 0;
+          for (uint32_t k = 0; k < m; ++k) sep += single[k];
+          if (fmk <= sep) {
+            plan = std::move(fused);
+            mk = fmk;
+            n = m;
+            break;
+          }
+        }
       }
-      // LPT: largest cost first onto the least loaded warp
-      std::vector<uint32_t> order(units.size());
-      std::iota(order.begin(), order.end(), 0u);
-      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return units[a].c > units[b].c; });
-      std::vector<double> load(NW, 0.0);
-      std::vector<std::vector<uint32_t>> perWarp(NW);  // unit indices
-      for (uint32_t u : order) {
-        uint32_t w = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
-        load[w] += units[u].c;
-        perWarp[w].push_back(u);
-      }
-      total += *std::max_element(load.begin(), load.end());
-      // does this level need a block barrier first?
+      total += mk;
+      // does this block need a block barrier first?
       bool need = lv == 0;
       if (!need) {
         for (uint32_t w = 0; w < NW && !need; ++w)
-          for (uint32_t u : perWarp[w]) {
-            const uint32_t i = units[u].i;
-            for (uint32_t s : mps[i].reads)
+          for (const Unit &un : plan[w]) {
+            const MPartRef &r = levels[un.lv][un.i];
+            for (uint32_t s : r.reads)
               if (lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) { need = true; break; }
             if (need) break;
-            for (uint32_t s : mps[i].writes)
+            for (uint32_t s : r.writes)
               if ((lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) || (readersMask[s] & ~(1u << w))) { need = true; break; }
             if (need) break;
           }
@@ -681,10 +799,10 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32
       // counts as written by each of them (the last one recorded): every
       // later access from another warp then needs a barrier
       for (uint32_t w = 0; w < NW; ++w)
-        for (uint32_t u : perWarp[w]) {
-          const uint32_t i = units[u].i;
-          for (uint32_t s : mps[i].reads) { readersMask[s] |= 1u << w; touched.push_back(s); }
-          for (uint32_t s : mps[i].writes) {
+        for (const Unit &un : plan[w]) {
+          const MPartRef &r = levels[un.lv][un.i];
+          for (uint32_t s : r.reads) { readersMask[s] |= 1u << w; touched.push_back(s); }
+          for (uint32_t s : r.writes) {
             if (lastWriter[s] >= 0 && lastWriter[s] != int32_t(w)) lastWriter[s] = int32_t(NW);  // several warps
             else lastWriter[s] = int32_t(w);
             touched.push_back(s);
@@ -695,36 +813,41 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32
       while (sw.size() % 4) sw.push_back(0);
       const uint32_t blk = uint32_t(sw.size());
       uint32_t nUnits = 0;
-      for (uint32_t w = 0; w < NW; ++w) nUnits += uint32_t(perWarp[w].size());
+      for (uint32_t w = 0; w < NW; ++w) nUnits += uint32_t(plan[w].size());
       sw.push_back(need ? 1u : 0u);
       uint32_t acc = 0;
       for (uint32_t w = 0; w < NW; ++w) {
         sw.push_back(acc);
-        acc += uint32_t(perWarp[w].size());
+        acc += uint32_t(plan[w].size());
       }
       sw.push_back(acc);
       const uint32_t unitBase = uint32_t(sw.size());
       sw.resize(sw.size() + nUnits, 0);
       while (sw.size() % 4) sw.push_back(0);
       uint32_t u = 0;
-      std::vector<uint32_t> recordAt(mps.size(), UINT32_MAX);  // one record per micro-partition
+      std::vector<std::vector<uint32_t>> recordAt(n);  // one record per micro-partition
+      for (uint32_t k = 0; k < n; ++k) recordAt[k].assign(levels[lv + k].size(), UINT32_MAX);
       for (uint32_t w = 0; w < NW; ++w)
-        for (uint32_t x : perWarp[w]) {
-          const Unit &un = units[x];
-          if (recordAt[un.i] == UINT32_MAX) {
-            recordAt[un.i] = uint32_t(sw.size()) - blk;
-            const MPartRef &r = mps[un.i];
+        for (const Unit &un : plan[w]) {
+          uint32_t &ra = recordAt[un.lv - lv][un.i];
+          if (ra == UINT32_MAX) {
+            ra = uint32_t(sw.size()) - blk;
+            const MPartRef &r = levels[un.lv][un.i];
             sw.insert(sw.end(), img.net.begin() + r.off, img.net.begin() + r.off + r.words);
             while (sw.size() % 4) sw.push_back(0);
           }
-          if (recordAt[un.i] > kUnitOffsetMask) throw Error(TGS_ERR_RESOURCES, "exec level too large");
-          sw[unitBase + u++] = recordAt[un.i] | (un.g0 << 24) | ((un.gn - 1) << 27);
+          if (ra > kUnitOffsetMask) throw Error(TGS_ERR_RESOURCES, "exec level too large");
+          sw[unitBase + u++] = ra | (un.g0 << 24) | ((un.gn - 1) << 27);
         }
       const uint32_t words = uint32_t(sw.size()) - blk;
       out.levelDesc.push_back(blk);
       out.levelDesc.push_back(words);
       out.maxLevelWords = std::max(out.maxLevelWords, words);
+      out.fusedLevels += n - 1;
+      ++blocks;
+      lv += n;
     }
+    pd.nLevels = blocks;  // exec-level blocks the kernel runs
     // L0 and last level scale with their op counts spread over the block
     total += double(pd.l0Count + pd.copySlots + 8 * pd.memWCount) / double(32 * NW) + 1.0;
     out.partCost[pid] = total;

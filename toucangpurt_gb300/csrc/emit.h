@@ -61,6 +61,13 @@ struct Schedule {
   std::vector<double> partCost;
   double makespan[2] = {0, 0};
   uint64_t barriers = 0, levels = 0;
+  uint64_t fusedLevels = 0;  // exec levels merged into the block before them (levels per barrier > 1)
+};
+
+// Schedule knobs (tgs_options.mpart_lanes / levels_per_barrier).
+struct SchedOpts {
+  uint32_t unitLanes = 32;       // LUTs a warp takes per unit of its level plan: 32, 64 or 128
+  uint32_t levelsPerBarrier = 1;  // exec levels one block may merge: 1, 2 or 4
 };
 
 // Word-wide evaluation of palette LUT ops.  A LUT op reads table entry
@@ -114,9 +121,12 @@ void buildImage(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, bool com
                 const ProbeList *probes = nullptr, bool packLanes = false, bool fastLuts = false);
 // cost: optional [part][level][mpart] predicted cost; null = gate count.
 // G: stream groups per item (special micro-partitions are split by group).
+// so: micro-partition size (LUT units bundled per warp) and levels per
+// barrier (consecutive exec levels merged into one block where every
+// dependency inside stays on one warp and the merged block is no slower).
 void buildSchedule(const toucanGPUSim::SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32_t G,
                    const std::vector<std::vector<std::vector<float>>> *cost, uint32_t nBlocks, uint32_t nGroupBlocks,
-                   Schedule &out);
+                   Schedule &out, const SchedOpts &so = SchedOpts());
 float gateCost(const MPartFeat &f);
 
 }  // namespace tgs

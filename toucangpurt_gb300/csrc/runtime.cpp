@@ -283,6 +283,13 @@ void configure(tgs_sim *h) {
     while (G > 1 && uint32_t(G) > h->groups) G >>= 1;
   }
   h->gpad = (h->groups + G - 1) / G * G;
+  SchedOpts so;
+  so.unitLanes = o.mpart_lanes ? o.mpart_lanes : 32u;
+  so.levelsPerBarrier = o.levels_per_barrier ? o.levels_per_barrier : 1u;
+  if (so.unitLanes != 32 && so.unitLanes != 64 && so.unitLanes != 128)
+    throw Error(TGS_ERR_ARG, "mpart_lanes must be 32, 64 or 128");
+  if (so.levelsPerBarrier != 1 && so.levelsPerBarrier != 2 && so.levelsPerBarrier != 4)
+    throw Error(TGS_ERR_ARG, "levels_per_barrier must be 1, 2 or 4");
   uint32_t NW = o.warps_per_block ? o.warps_per_block : autoWarps(h->img, uint32_t(G), h->spw);
   if (NW < 1 || NW > 32) throw Error(TGS_ERR_ARG, "warps_per_block must be 1 to 32");
   h->lc.spw = int(h->spw);
@@ -327,7 +334,7 @@ void configure(tgs_sim *h) {
                                        " groups needs " + std::to_string(kLutTablePadded + vpBytes) +
                                        " B of shared memory; lower groups_per_item");
   // first pass to learn the largest level block (independent of the block count)
-  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, 1, nGB, h->sched);
+  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, 1, nGB, h->sched, so);
   // Stage buffer size: the largest level, or a smaller size that still
   // stages nearly every level when it puts more blocks on an SM (levels
   // larger than the buffers are read from global memory; mixed 4M-LUT
@@ -383,7 +390,7 @@ void configure(tgs_sim *h) {
   }
   h->stageWords = stage;
   h->lc.blocks = uint32_t(std::max<size_t>(1, std::min<size_t>(size_t(perSM) * h->props.multiProcessorCount, maxItems)));
-  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, h->lc.blocks, nGB, h->sched);
+  buildSchedule(h->design, h->img, NW, uint32_t(G), costPtr, h->lc.blocks, nGB, h->sched, so);
 
   // Resident exec levels: the levels of every partition a block evaluates
   // (both regions, one contiguous range of the schedule per partition) are
@@ -988,7 +995,8 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
             t.blocks_per_sm = bps;
             t.resident_netlist = stagedOpt ? 2u : 0u;
             h->opt = t;
-            tgs_tune_trial tr{G, NW, bps, 0, 0, 0, -1.f};
+            tgs_tune_trial tr{G, NW, bps, 0, 0, 0, -1.f, base.mpart_lanes ? base.mpart_lanes : 32u,
+                              base.levels_per_barrier ? base.levels_per_barrier : 1u};
             bool fits = true;
             try {
               configure(h);
@@ -1029,6 +1037,43 @@ int tgs_autotune(tgs_sim *h, const tgs_tune_opts *opts, tgs_tune_trial *trials, 
     h->opt.blocks_per_sm = win.blocks_per_sm;
     h->opt.mode = win.mode;
     h->opt.resident_netlist = win.staged ? 0u : 2u;  // the default picks resident / staged as in the trial
+    // schedule knobs with the fastest launch configuration: micro-partition
+    // size x levels per barrier
+    {
+      const tgs_options launch = h->opt;
+      for (uint32_t lanes : {32u, 64u, 128u})
+        for (uint32_t lpbv : {1u, 2u, 4u}) {
+          if (lanes == win.mpart_lanes && lpbv == win.levels_per_barrier) continue;  // timed already
+          tgs_options t = launch;
+          t.mpart_lanes = lanes;
+          t.levels_per_barrier = lpbv;
+          h->opt = t;
+          tgs_tune_trial tr = win;
+          tr.mpart_lanes = lanes;
+          tr.levels_per_barrier = lpbv;
+          tr.ms_per_cycle = -1.f;
+          bool fits = true;
+          try {
+            configure(h);
+          } catch (const Error &e) {
+            if (e.code != TGS_ERR_RESOURCES && e.code != TGS_ERR_ARG) throw;
+            fits = false;
+          }
+          if (fits) {
+            tr.blocks = h->lc.blocks;
+            tr.staged = h->resWords ? 2u : h->stageWords ? 1u : 0u;
+            resetState(h);
+            fillParams(h);
+            runTimed(h, 0, warm, 0);
+            tr.ms_per_cycle = runTimed(h, warm, cycles, 0) / float(cycles);
+            if (tr.ms_per_cycle < win.ms_per_cycle) win = tr;
+          }
+          all.push_back(tr);
+        }
+      h->opt = launch;
+      h->opt.mpart_lanes = win.mpart_lanes;
+      h->opt.levels_per_barrier = win.levels_per_barrier;
+    }
     configure(h);
     resetState(h);
     h->cycleCnt = 0;
@@ -1866,6 +1911,7 @@ extern "C" int tgs_get_design_stats(const tgs_sim *h, tgs_design_stats *o) {
     o->streams_per_word = h->spw;
     o->block_barriers = h->sched.barriers;
     o->exec_levels = h->sched.levels;
+    o->fused_levels = uint32_t(h->sched.fusedLevels);
     o->makespan[0] = h->sched.makespan[0];
     o->makespan[1] = h->sched.makespan[1];
     o->smem_per_block = uint32_t(h->lc.smem);
