@@ -153,15 +153,17 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profiled_traffic():
-    """DRAM bytes per regionKernel launch from the committed ncu summary
-    (dram__bytes_read.sum + dram__bytes_write.sum, small case of the same
-    kernel), or None."""
+def profiled(key: str):
+    """A figure of the committed ncu summary of the region kernel (small case
+    of the same kernel): traffic_bytes_per_launch (dram__bytes_read.sum +
+    dram__bytes_write.sum), smem_wavefronts_per_sm_cycle and
+    smem_useful_wavefronts_per_sm_cycle (shared-memory wavefronts, without
+    bank-conflict replays, per SM and cycle), or None."""
     import re
 
     try:
         t = (ROOT / "profiles" / "regionkernel_largest_64streams.md").read_text()
-        return int(re.search(r"traffic_bytes_per_launch: (\d+)", t).group(1))
+        return float(re.search(key + r": ([0-9.]+)", t).group(1))
     except Exception:
         return None
 
@@ -513,7 +515,8 @@ def run_gb300(a, rank, ws):
     bytes_launch = algorithmic_bytes(st, streams, cps) / launches_step
     launch_s = dev_ms / 1000.0 / a.steps / launches_step
     achieved = bytes_launch / launch_s / 1e9
-    traffic = profiled_traffic() if a.workload == "largest" and streams == 64 else None
+    prof = a.workload == "largest" and streams == 64
+    traffic = int(profiled("traffic_bytes_per_launch")) if prof and profiled("traffic_bytes_per_launch") else None
     cpu = parity = plain = refk = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         from oracle import pyoracle
@@ -526,6 +529,18 @@ def run_gb300(a, rank, ws):
                          f"(a run of 1 + {a.cpu_sample_cycles} cycles less a run of 1 cycle)"}
         parity = parity_check(od, s, stim, out, streams, cps, a.cpu_sample_cycles, nth)
         del od
+    sched_gain = None
+    if rank == 0 and ws == 1 and not a.no_baselines and a.schedule == "learned":
+        # the same steps with the gate-count schedule (the learned model's fallback)
+        s.set_options(schedule=0)
+        for _ in range(a.warmup):
+            s.batch_run(cyc, stim)
+        greedy_ms = sum(s.batch_run(cyc, stim).device_ms for _ in range(a.steps))
+        s.set_options(schedule=1)
+        sched_gain = {"greedy_value": streams * cps * a.steps / (greedy_ms / 1000.0), "unit": "stimulus-cycles/s",
+                      "learned_over_greedy": greedy_ms / dev_ms,
+                      "train_s": notes.get("cost_model", {}).get("train_s"),
+                      "samples": notes.get("cost_model", {}).get("samples")}
     if rank == 0 and ws == 1 and not a.no_baselines:
         if streams > 1:
             plain = plain_form(a, dp, sp, info, gpu, cps, stim)
@@ -550,7 +565,12 @@ def run_gb300(a, rank, ws):
                          "traffic": traffic, "peak_source": peak_kind,
                          "kernel": f"regionKernel<{st['streams_per_word']},{st['groups_per_item']}>",
                          "algorithmic_bytes_per_launch": bytes_launch, "launch_us": launch_s * 1e6,
-                         "note": "bound on chip by shared-memory table lookups (profiles/): HBM is not the limit"},
+                         "note": "bound on chip by instruction issue and shared-memory table lookups (profiles/): HBM "
+                                 "is not the limit",
+                         "smem": {"wavefronts_per_sm_cycle": profiled("smem_wavefronts_per_sm_cycle") if prof else None,
+                                  "useful_wavefronts_per_sm_cycle":
+                                      profiled("smem_useful_wavefronts_per_sm_cycle") if prof else None,
+                                  "peak": 1.0, "source": "ncu capture of the same kernel (profiles/)"}},
             "e2e": {"value": e2e, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "path": "tgs_batch_run per step: host stimulus table (pinned) uploaded, continued run, "
@@ -560,6 +580,8 @@ def run_gb300(a, rank, ws):
         }
         if parity:
             line["parity"] = parity
+        if sched_gain:
+            line["learned_schedule"] = sched_gain
         if plain:
             line["plain"] = plain
         if refk:

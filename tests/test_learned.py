@@ -90,12 +90,10 @@ def test_training_learns_costs_and_keeps_values_exact(mixed_design):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("packing", [0, 1])
-def test_learned_schedule_gain(mixed_design, packing):
-    """Measured cycle time of the learned schedule against the gate-count one
-    on the heterogeneous design (same streams, same cycles), with the narrow
-    control cones packed into full warps (the default) and as the design
-    file has them (one warp pass per 4-8-lane cone, where gate count is the
-    poorest guide to cost)."""
+def test_learned_schedule_no_regression(mixed_design, packing):
+    """On a small heterogeneous design, where every exec level holds about
+    as many units as a block has warps, the schedule has little to balance:
+    the learned one must not be slower than the gate-count one."""
     dp, sp, info = mixed_design
     n, cycles = 64, 60
     stim = sim.StimulusSpec(8, info["pi_ids"], info["pi_bits"])
@@ -110,4 +108,40 @@ def test_learned_schedule_gain(mixed_design, packing):
             t[name] = min(s.batch_run(cyc, stim, rolling=False).device_ms for _ in range(3))
     print(f"lane_packing={packing}: greedy {t['greedy']:.2f} ms, learned {t['learned']:.2f} ms, "
           f"gain {t['greedy'] / t['learned']:.3f}x")
-    assert t["learned"] <= t["greedy"] * 1.05
+    assert t["learned"] <= t["greedy"] * 1.02
+
+
+@pytest.mark.gpu
+def test_learned_schedule_gain_on_benchmarked_design(tmp_path, built):
+    """The benchmarked learned-partitioning workload: the mixed 4M-LUT design
+    (datapath, deep control, memory-heavy and high-fan-out regions) with 256
+    streams, about 8 items per partition spread over the blocks.  Gate count
+    mispredicts the cost of its micro-partitions (memory ports, vector ops,
+    word-wide palette ops, deep cones); the network, trained on about 200K
+    clock64 samples (every micro-partition, over several profiling passes),
+    balances blocks and warps by predicted cost.
+    Measured: 1.06x (31.0 ms against 33.0 ms for 40 cycles); asserted: a real
+    gain of at least 3 %."""
+    from toucangpurt_gb300 import workloads
+
+    dp, sp = tmp_path / "d.bin", tmp_path / "s.bin"
+    info = sim.generate(dp, sp, **workloads.design_config("learned"))
+    streams, cycles = 256, 40
+    stim = sim.StimulusSpec(8, info["pi_ids"], info["pi_bits"])
+    cyc = np.full(streams, cycles, np.uint32)
+    s, notes = workloads.bench_simulator("learned", dp, sp, streams=streams)
+    try:
+        cm = notes["cost_model"]
+        assert cm["samples"] >= 150_000  # per-micro-partition clock64 samples of several profiling passes
+        assert cm["val_corr"] > 0.9 and cm["val_corr"] > cm["gate_corr"]
+        t = {"greedy": [], "learned": []}
+        for _ in range(3):
+            for name, sched in (("greedy", sim.capi.SCHED_GREEDY), ("learned", sim.capi.SCHED_LEARNED)):
+                s.set_options(schedule=sched)
+                s.batch_run(cyc, stim, rolling=False)  # warm
+                t[name].append(min(s.batch_run(cyc, stim, rolling=False).device_ms for _ in range(2)))
+    finally:
+        s.cleanup()
+    g, l = min(t["greedy"]), min(t["learned"])
+    print(f"mixed 4M-LUT x {streams}: greedy {g:.2f} ms, learned {l:.2f} ms, gain {g / l:.3f}x, {cm}")
+    assert g / l >= 1.03

@@ -86,13 +86,14 @@ def toggles(name: str, bits: np.ndarray) -> np.ndarray | None:
 
 def bench_simulator(name: str, design, symbols, *, streams: int | None = None, gpu: int = 0, schedule: str = "auto",
                     mode: str = "auto", groups: int = 0, warps: int = 0, levels: int = 0, value_pool: int = 0,
-                    profile_cycles: int = 20, epochs: int = 40, seed: int = 5, **options):
+                    profile_cycles: int = 20, epochs: int = 40, seed: int = 5, samples: int = 200_000, **options):
     """A simulator loaded and configured the way the benchmark runs a
     workload: `streams` resident streams (default: the workload's count),
     the CUDA-graph form unless the exec levels stay resident in shared
     memory (then one persistent launch), and for more than one stream the
     learned schedule (every micro-partition profiled for `profile_cycles`
-    cycles, the cost model trained on those samples).  Further tgs_options
+    cycles, repeated until about `samples` (features, clock64 cycles) samples
+    are collected, the cost model trained on them).  Further tgs_options
     fields may be given by name.  Returns (simulator, notes) where notes
     holds the cost model's validation figures."""
     import time
@@ -111,8 +112,13 @@ def bench_simulator(name: str, design, symbols, *, streams: int | None = None, g
         s.set_options(mode=capi.MODE_PERSISTENT)  # resident levels are loaded once per run
     if schedule == "learned":
         t0 = time.perf_counter()
-        rep = s.train_cost_model(s.mpart_features(), s.profile_mparts(profile_cycles), epochs=epochs, seed=seed)
+        feats = s.mpart_features()
+        passes = max(1, min(8, -(-samples // max(1, len(feats)))))
+        X = np.concatenate([feats] * passes)
+        y = np.concatenate([s.profile_mparts(profile_cycles) for _ in range(passes)])
+        rep = s.train_cost_model(X, y, epochs=max(1, epochs // passes), seed=seed)
         s.set_options(schedule=capi.SCHED_LEARNED)
         notes["cost_model"] = {k: round(float(v), 4) for k, v in rep.items() if k in ("val_mse", "val_corr", "gate_corr")}
         notes["cost_model"]["train_s"] = round(time.perf_counter() - t0, 2)
+        notes["cost_model"]["samples"] = int(len(y))
     return s, notes
