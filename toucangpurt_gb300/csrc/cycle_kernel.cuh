@@ -571,51 +571,33 @@ __device__ __forceinline__ void evalMemRead(const KParams &p, const Words<SH> mp
 }
 
 // ---- exec-level staging ------------------------------------------------------
-// Two shared-memory buffers, one mbarrier each.  Thread 0 issues the bulk copy
-// of level lv + 1 right after the block barrier that opens level lv (so every
-// thread is done with the buffer's previous level); every thread waits on the
-// buffer's phase parity before reading it.  Waits are bounded.
+// Two shared-memory buffers: level lv + 1 is copied into one while level lv
+// runs from the other (stageCopy below).  mb0 is the block's setup mbarrier
+// (resident exec levels).
 struct Stage {
   uint32_t buf0;   // shared address of buffer 0; buffer b at buf0 + b * bytes
   uint32_t bytes;  // bytes of one buffer
-  uint32_t mb0;    // shared address of mbarrier 0; mbarrier b at mb0 + 8 * b
-  uint32_t phase;  // bit b: phase parity of buffer b's next completion
+  uint32_t mb0;    // shared address of mbarrier 0
 };
-
-__device__ __forceinline__ void stageIssue(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words) {
-  const uint32_t bytes = words * 4u;
-  const uint32_t dst = st.buf0 + b * st.bytes, mb = st.mb0 + 8u * b;
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(mb)
-               : "memory");
-}
 
 // A waiting thread is suspended by the hardware (up to this many ns per try)
 // instead of spinning: no issue slots are spent on the wait.
 constexpr uint32_t kStageSuspendNs = 20000;
 
-__device__ __forceinline__ bool stageWait(const KParams &p, Stage &st, uint32_t b) {
-  const uint32_t parity = (st.phase >> b) & 1u, mb = st.mb0 + 8u * b;
-  uint32_t done = 0;
-  unsigned long long t0 = 0;
-  for (uint32_t spin = 0; !done; ++spin) {
-    asm volatile(
-        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, P;\n\t}"
-        : "=r"(done)
-        : "r"(mb), "r"(parity), "r"(kStageSuspendNs)
-        : "memory");
-    if (!done) {
-      if (spin == 0) t0 = gtimer();
-      else if (gtimer() - t0 > p.timeoutNs) {
-        raiseErr(p, kErrTimeout, blockIdx.x, 0xFFFFFFFEu, b);
-        return false;
-      }
-    }
-  }
-  st.phase ^= 1u << b;
-  return true;
+// Cooperative staging: every thread of the block copies its 16-byte pieces of
+// a level block global -> shared with asynchronous copies through the load /
+// store path (no copy engine, no mbarrier); a thread waits for its own copies
+// right before the block barrier that opens the level, which then makes every
+// piece visible to every thread.  (Level blocks are whole 16-byte units at
+// 16-byte aligned offsets.)
+__device__ __forceinline__ void stageCopy(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words,
+                                          uint32_t tid, uint32_t nthr) {
+  const uint32_t dst = st.buf0 + b * st.bytes;
+  for (uint32_t k = tid; k < words / 4u; k += nthr)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u * k), "l"(src + 4u * k) : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
 }
+__device__ __forceinline__ void stageCopyWait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // The units a warp runs in one exec level (block = the level's words).
 template <int SPW, int G, bool SH>
@@ -717,9 +699,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
   uint2 nxt = d.nLevels > 1 ? __ldg(ld + 1) : zero2;
   const uint32_t x0 = cur.x;  // first level block of the partition (resident offset 0)
   // the first exec level streams in while the level-0 reads run
-  if (cap && tid == 0 && d.nLevels) {
-    if (cur.y <= cap) stageIssue(st, 0, p.sched + cur.x, cur.y);
-  }
+  if (cap && d.nLevels && cur.y <= cap) stageCopy(st, 0, p.sched + cur.x, cur.y, tid, nthr);
 
   // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
   {
@@ -733,6 +713,7 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
       copyInG<G>(vpAddr<G>(vp, r, 0), pool + size_t(s) * p.gpad + gb * G);
     }
   }
+  if (cap) stageCopyWait();  // the first level's pieces, before the barrier that publishes them
   __syncthreads();
   // resident levels: the block's copies were issued at setup and overlapped
   // the level-0 reads; on a (never expected) timeout the levels are read from
@@ -757,14 +738,14 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
       }
     }
     if (cap) {
-      if (lv > 0) __syncthreads();  // staged buffers are reused every second level
-      if (tid == 0 && lv + 1 < d.nLevels) {
-        if (nxt.y <= cap) stageIssue(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y);
+      // level lv's pieces (copied during level lv - 1) are complete and, after
+      // the barrier, visible; the buffers are reused every second level
+      if (lv > 0) {
+        stageCopyWait();
+        __syncthreads();
       }
-      // on a (never expected) wait timeout the level is read from global
-      // memory instead: same words, uniform control flow, and the error word
-      // ends the launch at the next grid barrier
-      staged = cur.y <= cap && stageWait(p, st, lv & 1u);
+      if (lv + 1 < d.nLevels && nxt.y <= cap) stageCopy(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y, tid, nthr);
+      staged = cur.y <= cap;
     } else if (lv > 0 && (__ldg(p.sched + cur.x) & 1u)) {
       __syncthreads();
     }
@@ -1304,7 +1285,6 @@ __device__ __forceinline__ bool setupBlock(const KParams &p, uint8_t *smem, unsi
   b.st.buf0 = base + kLutTablePadded;
   b.st.bytes = p.stageWords * 4u;
   b.st.mb0 = uint32_t(__cvta_generic_to_shared(&stageMbar[0]));
-  b.st.phase = 0;
   b.res = b.st.buf0 + 2u * b.st.bytes;
   b.vp = b.res + (RES ? 4u * p.resWords : 0u);
   b.resState = 0;
