@@ -584,10 +584,10 @@ struct Stage {
 // instead of spinning: no issue slots are spent on the wait.
 constexpr uint32_t kStageSuspendNs = 20000;
 
-// Cooperative staging: every thread of the block copies its 16-byte pieces of
-// a level block global -> shared with asynchronous copies through the load /
-// store path (no copy engine, no mbarrier); a thread waits for its own copies
-// right before the block barrier that opens the level, which then makes every
+// Staging: the threads of one warp copy the 16-byte pieces of a level block
+// global -> shared with asynchronous copies through the load / store path
+// (no copy engine, no mbarrier); a thread waits for its own copies right
+// before the block barrier that opens the level, which then makes every
 // piece visible to every thread.  (Level blocks are whole 16-byte units at
 // 16-byte aligned offsets.)
 __device__ __forceinline__ void stageCopy(const Stage &st, uint32_t b, const uint32_t *src, uint32_t words,
@@ -699,7 +699,9 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
   uint2 nxt = d.nLevels > 1 ? __ldg(ld + 1) : zero2;
   const uint32_t x0 = cur.x;  // first level block of the partition (resident offset 0)
   // the first exec level streams in while the level-0 reads run
-  if (cap && d.nLevels && cur.y <= cap) stageCopy(st, 0, p.sched + cur.x, cur.y, tid, nthr);
+  // (the block's last warp issues the pieces: the other warps go straight
+  // to their units instead of queueing copies behind the table lookups)
+  if (cap && d.nLevels && cur.y <= cap && warp == NW - 1) stageCopy(st, 0, p.sched + cur.x, cur.y, lane, 32u);
 
   // level 0: register / exchange reads (evalPartL0RegRead / ExgRead)
   {
@@ -744,7 +746,8 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
         stageCopyWait();
         __syncthreads();
       }
-      if (lv + 1 < d.nLevels && nxt.y <= cap) stageCopy(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y, tid, nthr);
+      if (lv + 1 < d.nLevels && nxt.y <= cap && warp == NW - 1)
+        stageCopy(st, (lv + 1) & 1u, p.sched + nxt.x, nxt.y, lane, 32u);
       staged = cur.y <= cap;
     } else if (lv > 0 && (__ldg(p.sched + cur.x) & 1u)) {
       __syncthreads();
