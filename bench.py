@@ -222,6 +222,17 @@ def cpu_cycles_time(od, stim, streams, cycles, threads):
     return max((t2 - t1) - (t1 - t0), 1e-9)
 
 
+def cpu_sample(od, stim, streams, cycles, threads, min_s=0.5):
+    """(seconds, cycles) of a CPU sample of at least `cycles` cycles, grown
+    until it takes `min_s` or more: a small design's few cycles take
+    microseconds, below what the difference of two runs resolves."""
+    while True:
+        dt = cpu_cycles_time(od, stim, streams, cycles, threads)
+        if dt >= min_s or cycles >= 1 << 20:
+            return dt, cycles
+        cycles = min(1 << 20, cycles * max(2, min(64, int(1.5 * min_s / max(dt, 1e-5)) + 1)))
+
+
 def run_reference(a, rank, ws):
     """Reference arm: CPU evaluation of the workload on all host threads."""
     if rank != 0:
@@ -241,7 +252,8 @@ def run_reference(a, rank, ws):
 
     od = po.OracleDesign(dp, sp)
     stim = sim.StimulusSpec(1234, info["pi_ids"], info["pi_bits"], workloads.toggles(a.workload, info["pi_bits"]))
-    for _ in range(a.warmup):
+    _, cyc = cpu_sample(od, stim, streams, cyc, threads)
+    for _ in range(a.warmup - 1):
         cpu_cycles_time(od, stim, streams, cyc, threads)
     dt = sum(cpu_cycles_time(od, stim, streams, cyc, threads) for _ in range(a.steps))
     v = streams * cyc * a.steps / dt
@@ -408,7 +420,7 @@ def run_e2e(a, s, info, stim, streams, cps):
 def parity_check(od, s, stim, timed, streams, cps, cycles, threads):
     """The oracle against this library on the benchmark's own inputs: the
     per-cycle register digests of every stream over the first `cycles`
-    cycles of a timed step, and the final register, memory and rolling
+    cycles of the run's first step, and the final register, memory and rolling
     digests of a separate `cycles`-cycle run (memories included)."""
     c = max(1, min(cycles, cps))
     ref = od.run(np.full(streams, c, np.uint32), stim, threads=threads, cycle_digests=True)
@@ -420,7 +432,7 @@ def parity_check(od, s, stim, timed, streams, cps, cycles, threads):
         if not np.array_equal(getattr(short, k), ref[k]):
             bad.append(k)
     return {"result": "bit-exact" if not bad else "MISMATCH: " + ", ".join(bad), "against": "CPU oracle",
-            "checked": f"{streams} streams x {c} cycles: per-cycle register digests of a timed step; final register, "
+            "checked": f"{streams} streams x {c} cycles: per-cycle register digests of the run's first step; final register, "
                        f"memory and rolling digests and stop cycles of a {c}-cycle run"}
 
 
@@ -488,18 +500,27 @@ def run_gb300(a, rank, ws):
     toggle = workloads.toggles(a.workload, info["pi_bits"])
     stim = sim.StimulusSpec(1000 + rank, info["pi_ids"], info["pi_bits"], toggle)
     cyc = np.full(streams, cps, np.uint32)
-    for _ in range(a.warmup):
-        s.batch_run(cyc, stim, cycle_digests=True)
+    # step 0 starts from the initial state (the oracle checks it); every later
+    # step, warm-up and timed, continues the run from the previous one, so the
+    # timed steps cover cycles W*cps .. (W+K)*cps of one long run
+    first = s.batch_run(cyc, stim, cycle_digests=True)
+    for _ in range(a.warmup - 1):
+        s.batch_run(cyc, stim, cycle_digests=True, continue_=True)
     barrier(ws)
     clk = Clocks(gpu)
     dev_ms = 0.0
     launches = 0
     for _ in range(a.steps):
-        out = s.batch_run(cyc, stim, cycle_digests=True)
+        out = s.batch_run(cyc, stim, cycle_digests=True, continue_=True)
         dev_ms += out.device_ms
         launches += out.launches
     clocks = clk.stop()
     barrier(ws)
+    # the continued steps against one uninterrupted run of the same length
+    before = max(1, a.warmup)  # steps run before the timed ones
+    whole = s.batch_run(np.full(streams, cps * (before + a.steps), np.uint32), stim, cycle_digests=True)
+    continued = bool(np.array_equal(whole.cycle_digest[:, -cps:], out.cycle_digest))
+    del whole
     e2e_s, h2d, d2h = run_e2e(a, s, info, stim, streams, cps)
     barrier(ws)
     dev_s = allreduce_max(dev_ms / 1000.0, ws)
@@ -508,10 +529,12 @@ def run_gb300(a, rank, ws):
     value = total_sc / dev_s
     e2e = total_sc / wall_s
     peak, peak_kind = measured_peak()
-    # the dominant kernel: one regionKernel launch per region and cycle; the
-    # device time of a step is the step's region launches (advance and
-    # stimulus launches are ~0.01 % of it, profiles/)
-    launches_step = 2 * cps
+    # the dominant kernel: one regionKernel launch per region and cycle (graph
+    # form) or one cycleKernel launch per step (persistent form); the device
+    # time of a step is those launches (advance and stimulus launches are
+    # ~0.01 % of it, profiles/)
+    graph = s.options()["mode"] == 1
+    launches_step = 2 * cps if graph else 1
     bytes_launch = algorithmic_bytes(st, streams, cps) / launches_step
     launch_s = dev_ms / 1000.0 / a.steps / launches_step
     achieved = bytes_launch / launch_s / 1e9
@@ -523,19 +546,23 @@ def run_gb300(a, rank, ws):
 
         nth = cpu_threads(info, streams)
         od = pyoracle.OracleDesign(dp, sp)
-        cdt = cpu_cycles_time(od, stim, streams, a.cpu_sample_cycles, nth)
-        cpu = {"value": streams * a.cpu_sample_cycles / cdt, "unit": "stimulus-cycles/s", "cores": nth, "kind": "port",
-               "sample": f"{streams} streams x {a.cpu_sample_cycles} cycle(s) of the same design, {cdt:.1f} s "
-                         f"(a run of 1 + {a.cpu_sample_cycles} cycles less a run of 1 cycle)"}
-        parity = parity_check(od, s, stim, out, streams, cps, a.cpu_sample_cycles, nth)
+        cdt, ccyc = cpu_sample(od, stim, streams, a.cpu_sample_cycles, nth)
+        cpu = {"value": streams * ccyc / cdt, "unit": "stimulus-cycles/s", "cores": nth, "kind": "port",
+               "sample": f"{streams} streams x {ccyc} cycle(s) of the same design, {cdt:.1f} s "
+                         f"(a run of 1 + {ccyc} cycles less a run of 1 cycle)"}
+        parity = parity_check(od, s, stim, first, streams, cps, a.cpu_sample_cycles, nth)
+        parity["continued_steps"] = ("equal to one uninterrupted run" if continued else "MISMATCH against one "
+                                     "uninterrupted run") + f" (per-cycle register digests, cycles " \
+                                    f"{before * cps}..{(before + a.steps) * cps - 1})"
         del od
     sched_gain = None
     if rank == 0 and ws == 1 and not a.no_baselines and a.schedule == "learned":
         # the same steps with the gate-count schedule (the learned model's fallback)
         s.set_options(schedule=0)
-        for _ in range(a.warmup):
-            s.batch_run(cyc, stim)
-        greedy_ms = sum(s.batch_run(cyc, stim).device_ms for _ in range(a.steps))
+        s.batch_run(cyc, stim)
+        for _ in range(a.warmup - 1):
+            s.batch_run(cyc, stim, continue_=True)
+        greedy_ms = sum(s.batch_run(cyc, stim, continue_=True).device_ms for _ in range(a.steps))
         s.set_options(schedule=1)
         sched_gain = {"greedy_value": streams * cps * a.steps / (greedy_ms / 1000.0), "unit": "stimulus-cycles/s",
                       "learned_over_greedy": greedy_ms / dev_ms,
@@ -545,7 +572,7 @@ def run_gb300(a, rank, ws):
         if streams > 1:
             plain = plain_form(a, dp, sp, info, gpu, cps, stim)
             plain["batched_over_plain"] = value / plain["value"]
-        refk = reference_kernel(dp, sp, info, stim, out, min(cps, a.ref_cycles))
+        refk = reference_kernel(dp, sp, info, stim, first, min(cps, a.ref_cycles))
         if "value" in refk:
             refk["batched_over_reference_kernel"] = value / refk["value"]
     if rank == 0:
@@ -563,7 +590,8 @@ def run_gb300(a, rank, ws):
             "lut_evals_per_s": value * st["lut_ops"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": f"regionKernel<{st['streams_per_word']},{st['groups_per_item']}>",
+                         "kernel": f"{'regionKernel' if graph else 'cycleKernel'}<{st['streams_per_word']},"
+                                   f"{st['groups_per_item']}>",
                          "algorithmic_bytes_per_launch": bytes_launch, "launch_us": launch_s * 1e6,
                          "note": "bound on chip by instruction issue and shared-memory table lookups (profiles/): HBM "
                                  "is not the limit",
