@@ -91,6 +91,27 @@ def test_exec_level_sources(designs, name, levels, mode):
     _compare(got2, ref)
 
 
+@pytest.mark.parametrize("name", ["small", "wide3op", "mixed", "deep_cones"])
+@pytest.mark.parametrize("levels", [0, 1, 3])  # auto, resident, staged
+@pytest.mark.parametrize("mode", [0, 1])  # persistent, graph
+@pytest.mark.parametrize("value_pool", [0, 1])  # renumbered (slot immediates), the design's numbering
+def test_single_stream_levels(designs, name, levels, mode, value_pool):
+    """One stream per word: resident exec levels take the path that reads and
+    decodes each warp's next unit during the current level (one-level compact
+    LUT records over slot immediates; every other unit, and the design's own
+    slot numbering, through the general path).  Bit-exact in every form."""
+    dp, sp, info = designs[name]
+    cycles = np.full(1, 40, np.uint32)
+    stim = _stim(info, seed=21)
+    with sim.Simulator(n_streams=1, resident_netlist=levels, mode=mode, value_pool=value_pool) as s:
+        s.init(0, dp, sp, False, False)
+        got = s.batch_run(cycles, stim, cycle_digests=True)
+        got2 = s.batch_run(cycles, stim, cycle_digests=True)
+    ref = pyoracle.OracleDesign(dp, sp).run(cycles, stim, cycle_digests=True)
+    _compare(got, ref)
+    _compare(got2, ref)
+
+
 @pytest.mark.parametrize("warps", [0, 3, 4, 6, 12, 16, 32])
 def test_warps_per_block(designs, warps):
     dp, sp, info = designs["wide3op"]

@@ -600,27 +600,32 @@ __device__ __forceinline__ void stageCopy(const Stage &st, uint32_t b, const uin
 __device__ __forceinline__ void stageCopyWait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // The units a warp runs in one exec level (block = the level's words).
+// Unit u of a level block (unit word: record offset | first group << 24 |
+// (groups - 1) << 27).
+template <int SPW, int G, bool SH>
+__device__ __forceinline__ void runUnit(const KParams &p, const PartDesc &d, const Words<SH> blk, const Words<SH> units,
+                                        uint32_t u, uint32_t vp, uint32_t tab, uint32_t lane, uint32_t gb) {
+  const uint32_t uw = units[u];
+  const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
+  const uint32_t hdr = mp[0];
+  if ((hdr & 3u) == kMPLut) {
+    evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0);  // always every group
+  } else {
+    const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
+    if ((hdr & 3u) == kMPVecRead) evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
+    else if ((hdr & 3u) == kMPVecOp) evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
+    else evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn);
+  }
+  __syncwarp();
+}
+
 template <int SPW, int G, bool SH>
 __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, const Words<SH> blk, uint32_t vp,
                                          uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
   const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
   const Words<SH> units = blk.at(2 + NW);
   if (!(p.flags & kFlagProfileMP)) {
-    for (uint32_t u = ub; u < ue; ++u) {
-      // unit word: record offset | first group << 24 | (groups - 1) << 27
-      const uint32_t uw = units[u];
-      const Words<SH> mp = blk.at(uw & kUnitOffsetMask);
-      const uint32_t hdr = mp[0];
-      if ((hdr & 3u) == kMPLut) {
-        evalLut<SPW, G, SH>(mp, hdr, vp, tab, lane, p.constSlots != 0);  // always every group
-      } else {
-        const uint32_t g0 = (uw >> 24) & 7u, gn = ((uw >> 27) & 7u) + 1u;
-        if ((hdr & 3u) == kMPVecRead) evalVecRead<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
-        else if ((hdr & 3u) == kMPVecOp) evalVecOp<SPW, G, SH>(p, d, mp, hdr, vp, lane, g0, gn);
-        else evalMemRead<SPW, G, SH>(p, mp, hdr, vp, lane, gb, g0, gn);
-      }
-      __syncwarp();
-    }
+    for (uint32_t u = ub; u < ue; ++u) runUnit<SPW, G, SH>(p, d, blk, units, u, vp, tab, lane, gb);
     return;
   }
   // the same with clock64 around every unit (cost-model samples)
@@ -642,6 +647,147 @@ __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, co
       atomicAdd(p.mpCycles + id, (unsigned long long)(clock64() - tm));
       atomicAdd(p.mpCount + id, gn);  // groups evaluated
     }
+  }
+}
+
+// ---- single stream, resident exec levels -------------------------------------
+// With one stream per word a warp has one table lookup per lane and level,
+// so a level is a chain of dependent shared-memory reads (unit list, unit
+// word, header, lane record, operands, table) and instruction latencies, not
+// throughput.  Resident level blocks do not change after the block set-up,
+// so the first unit of a warp's NEXT level is read and decoded while the
+// current level runs; after the level barrier only the operand loads, the
+// lookup and the write-back are left.  A first unit that is not a one-level
+// compact LUT record over a pool with slot immediates (the common case)
+// runs through the general unit path, as do a warp's further units.
+
+// A word of a resident level block: the block never changes after the set-up
+// (it is read only after the resident-copy wait, through addresses derived
+// from its result), so the load is not volatile and the compiler may move it
+// among the value-pool accesses.
+__device__ __forceinline__ uint32_t ldsFixed(uint32_t a) {
+  uint32_t v;
+  asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint2 ldsFixed2(uint32_t a) {
+  uint2 v;
+  asm("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+  return v;
+}
+
+// Predicated accesses: no access where c is false.  ldsIf keeps `v` there;
+// value-pool words are volatile as in ldsU32 / stsU32.
+__device__ __forceinline__ uint32_t ldsIf(uint32_t a, bool c, uint32_t v) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.shared.u32 %0, [%1];\n\t}"
+               : "+r"(v)
+               : "r"(a), "r"(uint32_t(c)));
+  return v;
+}
+__device__ __forceinline__ uint2 ldsFixed2If(uint32_t a, bool c) {
+  uint2 v = make_uint2(0u, 0u);
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.shared.v2.u32 {%0, %1}, [%2];\n\t}"
+      : "+r"(v.x), "+r"(v.y)
+      : "r"(a), "r"(uint32_t(c)));
+  return v;
+}
+__device__ __forceinline__ void stsIf(uint32_t a, uint32_t v, bool c) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.shared.u32 [%0], %1;\n\t}" ::"r"(a), "r"(v),
+               "r"(uint32_t(c))
+               : "memory");
+}
+
+// A warp's part of one exec level, its first unit decoded.
+struct WarpLevel1 {
+  uint32_t ub, ue;    // the warp's units
+  bool sync;          // the level starts with a block barrier
+  bool simple;        // first unit: one-level compact LUT record, slot operands
+  bool act, st;       // the lane evaluates a LUT / writes an entry back (simple only)
+  uint32_t aA, aB, aC, lut, wA;  // operand and write-back slot addresses, lutIndex (0: pass c through)
+};
+
+// The words of level block blk a warp starts from: flags, unit range, and
+// the first unit's record offset (the flags word when the warp has no unit,
+// so every address stays inside the block).
+struct WarpLevelHead {
+  uint32_t flags, ub, ue, mp;
+};
+
+// Decodes the first unit of a warp's level (hdr: its header word).
+__device__ __forceinline__ WarpLevel1 decodeWarpLevel1(const WarpLevelHead &h, uint32_t hdr, uint32_t vp,
+                                                       uint32_t lane, bool constSlots) {
+  WarpLevel1 r;
+  r.sync = (h.flags & 1u) != 0u;
+  r.ub = h.ub;
+  r.ue = h.ue;
+  const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
+  r.simple = h.ub < h.ue && constSlots && (hdr & 3u) == kMPLut && (hdr & kMPCompact) != 0u &&
+             (hdr & kMPFastTop) == 0u && nMid == 0u;
+  r.act = r.simple && lane < W;
+  r.st = r.simple && lane < nWB;
+  // compact lane pair (as evalLutPass): a | b << 12 | (c & 255) << 24,
+  // c >> 8 | write-back slot << 4 | lutIndex << 16; a lane without a LUT
+  // (lane >= W) writes 0 to slot 0 when lane < nWB, as evalLutPass does
+  const uint2 w = ldsFixed2If(h.mp + 4u * kMPHeaderWords + 8u * lane, r.act);
+  r.lut = w.y >> 16;
+  r.aA = vp + 4u * (w.x & 0xFFFu);
+  r.aB = vp + 4u * ((w.x >> 12) & 0xFFFu);
+  r.aC = vp + 4u * ((w.x >> 24) | ((w.y & 15u) << 8));
+  r.wA = vp + 4u * ((w.y >> 4) & 0xFFFu);
+  return r;
+}
+
+__device__ __forceinline__ WarpLevelHead readWarpLevelHead(uint32_t blk, uint32_t warp) {
+  WarpLevelHead h;
+  h.flags = ldsFixed(blk);
+  h.ub = ldsFixed(blk + 4u * (1u + warp));
+  h.ue = ldsFixed(blk + 4u * (2u + warp));
+  h.mp = blk;
+  return h;
+}
+
+// Every exec level of one single-stream item, levels resident at res (the
+// partition's first block at x0).  Same results as runLevel level by level.
+// Per level the source order interleaves two dependent chains -- this
+// level's operands, lookup and write-back, and the next level's unit range,
+// unit word, header and lane record -- so that their shared-memory
+// latencies overlap; the accesses are predicated instead of branched so the
+// chains stay in one basic block.
+__device__ __forceinline__ void runLevelsSingle(const KParams &p, const PartDesc &d, uint32_t res, uint32_t x0,
+                                                const uint2 *__restrict__ ld, uint2 cur, uint2 nxt, uint32_t vp,
+                                                uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
+  const bool cs = p.constSlots != 0;
+  const uint2 zero2 = make_uint2(0u, 0u);
+  WarpLevel1 now;
+  {
+    const uint32_t blk = res + 4u * (cur.x - x0);
+    WarpLevelHead h = readWarpLevelHead(blk, warp);
+    if (h.ub < h.ue) h.mp = blk + 4u * (ldsFixed(blk + 4u * (2u + NW + h.ub)) & kUnitOffsetMask);
+    now = decodeWarpLevel1(h, ldsFixed(h.mp), vp, lane, cs);
+  }
+  for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
+    const uint2 after = lv + 2 < d.nLevels ? __ldg(ld + lv + 2) : zero2;
+    const uint32_t blk = res + 4u * (cur.x - x0);
+    // the next level's block (this one again after the last level: the
+    // reads stay in bounds and their results are not used)
+    const uint32_t nb = lv + 1 < d.nLevels ? res + 4u * (nxt.x - x0) : blk;
+    if (lv > 0 && now.sync) __syncthreads();
+    const uint32_t A = ldsIf(now.aA, now.act, 0u), B = ldsIf(now.aB, now.act, 0u), C = ldsIf(now.aC, now.act, 0u);
+    WarpLevelHead h = readWarpLevelHead(nb, warp);
+    const uint32_t uw = ldsFixed(h.ub < h.ue ? nb + 4u * (2u + NW + h.ub) : nb);
+    // inactive lanes: A = B = C = 0 and lut = 0, an address inside the table
+    const uint32_t T = ldsTab(tab + now.lut + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
+    if (h.ub < h.ue) h.mp = nb + 4u * (uw & kUnitOffsetMask);
+    const uint32_t hdr = ldsFixed(h.mp);
+    stsIf(now.wA, now.lut ? T : C, now.st);
+    __syncwarp();
+    const WarpLevel1 next = decodeWarpLevel1(h, hdr, vp, lane, cs);
+    for (uint32_t u = now.ub + (now.simple ? 1u : 0u); u < now.ue; ++u)
+      runUnit<1, 1, true>(p, d, Words<true>{nullptr, blk}, Words<true>{nullptr, blk + 4u * (2u + NW)}, u, vp, tab,
+                          lane, gb);
+    now = next;
+    cur = nxt;
+    nxt = after;
   }
 }
 
@@ -726,7 +872,14 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
   }
 
   // exec levels: warp w runs the units the schedule gave it
-  for (uint32_t lv = 0; lv < d.nLevels; ++lv) {
+  bool levelsDone = false;
+  if constexpr (SPW == 1 && G == 1 && RES) {
+    if (res && !(p.flags & kFlagProfileMP)) {
+      runLevelsSingle(p, d, res, x0, ld, cur, nxt, vp, tab, lane, warp, NW, gb);
+      levelsDone = true;
+    }
+  }
+  for (uint32_t lv = 0; lv < d.nLevels && !levelsDone; ++lv) {
     const uint2 after = lv + 2 < d.nLevels ? __ldg(ld + lv + 2) : zero2;
     bool staged = false;
     if constexpr (RES) {
