@@ -650,15 +650,16 @@ __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, co
   }
 }
 
-// ---- single stream, resident exec levels -------------------------------------
-// With one stream per word a warp has one table lookup per lane and level,
-// so a level is a chain of dependent shared-memory reads (unit list, unit
-// word, header, lane record, operands, table) and instruction latencies, not
-// throughput.  Resident level blocks do not change after the block set-up,
-// so the first unit of a warp's NEXT level is read and decoded while the
-// current level runs; after the level barrier only the operand loads, the
-// lookup and the write-back are left.  A first unit that is not a one-level
-// compact LUT record over a pool with slot immediates (the common case)
+// ---- one stream group per item, resident exec levels -------------------------
+// With one group per item (a single stream, or 8 streams per word and G = 1,
+// e.g. thousands of queued streams of a small design) a warp has one word
+// per lane and level, so a level is a chain of dependent shared-memory reads
+// (unit range, unit word, header, lane record, operands, table) and
+// instruction latencies, not throughput.  Resident level blocks do not change
+// after the block set-up, so the first unit of a warp's NEXT level is read
+// and decoded while the current level runs; after the level barrier only the
+// operand loads, the lookup and the write-back are left.  A first unit that
+// is not a one-level compact table record over a pool with slot immediates
 // runs through the general unit path, as do a warp's further units.
 
 // A word of a resident level block: the block never changes after the set-up
@@ -746,13 +747,15 @@ __device__ __forceinline__ WarpLevelHead readWarpLevelHead(uint32_t blk, uint32_
   return h;
 }
 
-// Every exec level of one single-stream item, levels resident at res (the
-// partition's first block at x0).  Same results as runLevel level by level.
+// Every exec level of one item of one stream group (G = 1), levels resident
+// at res (the partition's first block at x0).  Same results as runLevel
+// level by level.
 // Per level the source order interleaves two dependent chains -- this
 // level's operands, lookup and write-back, and the next level's unit range,
 // unit word, header and lane record -- so that their shared-memory
 // latencies overlap; the accesses are predicated instead of branched so the
 // chains stay in one basic block.
+template <int SPW>
 __device__ __forceinline__ void runLevelsSingle(const KParams &p, const PartDesc &d, uint32_t res, uint32_t x0,
                                                 const uint2 *__restrict__ ld, uint2 cur, uint2 nxt, uint32_t vp,
                                                 uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
@@ -776,15 +779,15 @@ __device__ __forceinline__ void runLevelsSingle(const KParams &p, const PartDesc
     WarpLevelHead h = readWarpLevelHead(nb, warp);
     const uint32_t uw = ldsFixed(h.ub < h.ue ? nb + 4u * (2u + NW + h.ub) : nb);
     // inactive lanes: A = B = C = 0 and lut = 0, an address inside the table
-    const uint32_t T = ldsTab(tab + now.lut + (((A & 15u) << 8) | ((B & 15u) << 4) | (C & 15u)));
+    const uint32_t T = lookup<SPW>(tab, now.lut, A, B, C);
     if (h.ub < h.ue) h.mp = nb + 4u * (uw & kUnitOffsetMask);
     const uint32_t hdr = ldsFixed(h.mp);
     stsIf(now.wA, now.lut ? T : C, now.st);
     __syncwarp();
     const WarpLevel1 next = decodeWarpLevel1(h, hdr, vp, lane, cs);
     for (uint32_t u = now.ub + (now.simple ? 1u : 0u); u < now.ue; ++u)
-      runUnit<1, 1, true>(p, d, Words<true>{nullptr, blk}, Words<true>{nullptr, blk + 4u * (2u + NW)}, u, vp, tab,
-                          lane, gb);
+      runUnit<SPW, 1, true>(p, d, Words<true>{nullptr, blk}, Words<true>{nullptr, blk + 4u * (2u + NW)}, u, vp, tab,
+                            lane, gb);
     now = next;
     cur = nxt;
     nxt = after;
@@ -873,9 +876,9 @@ __device__ void evalItem(const KParams &p, uint32_t item, uint32_t vp, uint32_t 
 
   // exec levels: warp w runs the units the schedule gave it
   bool levelsDone = false;
-  if constexpr (SPW == 1 && G == 1 && RES) {
+  if constexpr (G == 1 && RES) {
     if (res && !(p.flags & kFlagProfileMP)) {
-      runLevelsSingle(p, d, res, x0, ld, cur, nxt, vp, tab, lane, warp, NW, gb);
+      runLevelsSingle<SPW>(p, d, res, x0, ld, cur, nxt, vp, tab, lane, warp, NW, gb);
       levelsDone = true;
     }
   }
