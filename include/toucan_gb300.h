@@ -309,6 +309,13 @@ int tgs_batch_run(tgs_sim *h, const tgs_batch *job, tgs_batch_result *res);
 int tgs_host_alloc(size_t bytes, void **out);
 int tgs_host_free(void *p);
 
+/* Releases everything the library holds on `device` (cudaDeviceReset
+ * through the library's own CUDA runtime: the device's primary context is
+ * destroyed with every allocation in it, the caller's included, and
+ * re-created on the next use).  Destroy every handle on the device first;
+ * page-locked buffers from tgs_host_alloc are freed with the context. */
+int tgs_device_reset(int device);
+
 /* ---- design statistics and launch shape (new) ------------------------- */
 typedef struct tgs_design_stats {
   uint64_t lut_ops;          /* table lookups (lutIndex != 0) */

@@ -170,6 +170,7 @@ SIGNATURES = {
     "tgs_get_design_stats": [C.c_void_p, C.POINTER(DesignStats)],
     "tgs_host_alloc": [C.c_size_t, C.POINTER(C.c_void_p)],
     "tgs_host_free": [C.c_void_p],
+    "tgs_device_reset": [C.c_int],
     "tgs_num_mparts": [C.c_void_p, u32p],
     "tgs_mpart_features": [C.c_void_p, C.POINTER(C.c_float), C.c_uint32],
     "tgs_profile_mparts": [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_uint32],

@@ -170,12 +170,10 @@ cudaError_t mlpForward(const float *params, const float *X, uint32_t n, float *o
 cudaError_t mlpGrad(const float *params, const float *X, const float *y, const uint32_t *idx, uint32_t n, float scale,
                     float *grad, float *loss, cudaStream_t st) {
   if (!n) return cudaSuccess;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(mlpGradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlpGradSmem()));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // set on every call: the attribute belongs to the current device's context
+  // (another device, or a context re-created after a reset, starts without it)
+  cudaError_t e = cudaFuncSetAttribute(mlpGradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mlpGradSmem()));
+  if (e != cudaSuccess) return e;
   const uint32_t blocks = std::min<uint32_t>(304, (n + kWarps - 1) / kWarps);
   mlpGradKernel<<<blocks, 32 * kWarps, mlpGradSmem(), st>>>(params, X, y, idx, n, scale, grad, loss);
   return cudaGetLastError();

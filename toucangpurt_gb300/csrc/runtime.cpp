@@ -2063,6 +2063,13 @@ extern "C" int tgs_host_free(void *p) {
   });
 }
 
+extern "C" int tgs_device_reset(int device) {
+  return guard([&] {
+    TGS_CUDA(cudaSetDevice(device));
+    TGS_CUDA(cudaDeviceReset());
+  });
+}
+
 // ---- learned cost model ---------------------------------------------------------
 namespace {
 void requireModel(tgs_sim *h) {
