@@ -91,7 +91,8 @@ typedef struct tgs_options {
                                 block without a block barrier between them where every dependency among their
                                 micro-partitions stays on one warp and the merged block is scheduled no longer than
                                 the levels apart (chains of narrow cones); values are unchanged */
-  uint32_t reserved[1];
+  uint32_t stage_words;      /* upper bound of a stage buffer in 32-bit words (0, the default: sized by the
+                                library); exec levels larger than the buffers are read from global memory */
 } tgs_options;
 
 #define TGS_SCHED_GREEDY 0u

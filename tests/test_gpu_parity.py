@@ -95,21 +95,46 @@ def test_exec_level_sources(designs, name, levels, mode):
 @pytest.mark.parametrize("levels", [0, 1, 3])  # auto, resident, staged
 @pytest.mark.parametrize("mode", [0, 1])  # persistent, graph
 @pytest.mark.parametrize("value_pool", [0, 1])  # renumbered (slot immediates), the design's numbering
-def test_single_stream_levels(designs, name, levels, mode, value_pool):
-    """One stream per word: resident exec levels take the path that reads and
-    decodes each warp's next unit during the current level (one-level compact
-    LUT records over slot immediates; every other unit, and the design's own
-    slot numbering, through the general path).  Bit-exact in every form."""
+@pytest.mark.parametrize("streams", [1, 8])  # one stream per word / 8 streams in one group
+def test_single_stream_levels(designs, name, levels, mode, value_pool, streams):
+    """One stream group per item: resident exec levels take the path that
+    reads and decodes each warp's next unit during the current level (one-
+    level compact LUT records over slot immediates; every other unit, and the
+    design's own slot numbering, through the general path); staged and global
+    ones the general loop.  Bit-exact in every form."""
     dp, sp, info = designs[name]
-    cycles = np.full(1, 40, np.uint32)
+    cycles = np.full(streams, 40, np.uint32)
     stim = _stim(info, seed=21)
-    with sim.Simulator(n_streams=1, resident_netlist=levels, mode=mode, value_pool=value_pool) as s:
+    with sim.Simulator(n_streams=streams, groups_per_item=1, resident_netlist=levels, mode=mode,
+                       value_pool=value_pool) as s:
         s.init(0, dp, sp, False, False)
         got = s.batch_run(cycles, stim, cycle_digests=True)
         got2 = s.batch_run(cycles, stim, cycle_digests=True)
     ref = pyoracle.OracleDesign(dp, sp).run(cycles, stim, cycle_digests=True)
     _compare(got, ref)
     _compare(got2, ref)
+
+
+@pytest.mark.parametrize("name", ["wide3op", "mixed", "deep_cones"])
+@pytest.mark.parametrize("streams,groups", [(1, 1), (8, 1), (24, 2)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_small_stage_buffers(designs, name, streams, groups, mode):
+    """Stage buffers capped below the largest exec levels (stage_words):
+    those levels are read from global memory, the others staged; one-group
+    and multi-group items, both forms."""
+    dp, sp, info = designs[name]
+    cycles = np.full(streams, 30, np.uint32)
+    stim = _stim(info, seed=23)
+    with sim.Simulator(n_streams=streams, groups_per_item=groups, resident_netlist=3, mode=mode,
+                       stage_words=256) as s:
+        s.init(0, dp, sp, False, False)
+        st = s.design_stats()
+        assert 0 < st["stage_words"] <= 256
+        if name == "wide3op":
+            assert st["stage_words"] == 256  # some of its levels are larger
+        got = s.batch_run(cycles, stim, cycle_digests=True)
+    ref = pyoracle.OracleDesign(dp, sp).run(cycles, stim, cycle_digests=True)
+    _compare(got, ref)
 
 
 @pytest.mark.parametrize("warps", [0, 3, 4, 6, 12, 16, 32])

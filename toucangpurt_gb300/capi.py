@@ -41,7 +41,7 @@ class Options(C.Structure):
         ("barrier_timeout_ms", C.c_uint32), ("validate", C.c_uint32), ("resident_netlist", C.c_uint32),
         ("value_pool", C.c_uint32), ("capture_signals", C.c_uint32), ("lane_packing", C.c_uint32),
         ("fast_luts", C.c_uint32), ("mpart_lanes", C.c_uint32), ("levels_per_barrier", C.c_uint32),
-        ("reserved", C.c_uint32 * 1),
+        ("stage_words", C.c_uint32),
     ]
 
 

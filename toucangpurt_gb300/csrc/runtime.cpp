@@ -340,6 +340,7 @@ void configure(tgs_sim *h) {
   // larger than the buffers are read from global memory; mixed 4M-LUT
   // design: 4 -> 5 blocks per SM, 256K -> 310K stimulus-cycles/s)
   uint32_t stage = o.resident_netlist == 2 ? 0u : std::min<uint32_t>(h->sched.maxLevelWords, 4096u);
+  if (o.stage_words) stage = std::min<uint32_t>(stage, (o.stage_words + 3u) & ~3u);
   int perSM = shape(stage);
   if (stage) {
     std::vector<uint32_t> sizes;
