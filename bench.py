@@ -376,7 +376,11 @@ def run_gb300_queued(a, rank, ws, dp, sp, info, streams, schedule, gpu):
                        "groups_per_item": st["groups_per_item"], **notes},
             "lut_evals_per_s": total / dev_s * st["lut_ops"],
             "e2e": {"value": total / wall_s, "unit": "stimulus-cycles/s", "h2d_bytes_per_step": int(cyc.nbytes),
-                    "d2h_bytes_per_step": int(streams * 8 * 3)},
+                    "d2h_bytes_per_step": int(streams * 8 * 3),
+                    "path": "tgs_batch_run per step: stream lengths uploaded, each queued stream's inputs derived "
+                            "from its seed on the device (a host table of every stream's inputs would be "
+                            f"{int(cyc.sum()) * len(info['pi_ids']) / 1e9:.1f} GB per step), final register, "
+                            "memory and rolling digests read back"},
             "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
