@@ -103,9 +103,10 @@ def bench_simulator(name: str, design, symbols, *, streams: int | None = None, g
     streams = streams or RUNS[name]["streams"]
     if schedule == "auto":
         schedule = "learned" if streams > 1 else "greedy"
-    s = sim.Simulator(n_streams=streams, groups_per_item=groups, warps_per_block=warps, resident_netlist=levels,
-                      mode=capi.MODE_PERSISTENT if mode == "persistent" else capi.MODE_GRAPH, value_pool=value_pool,
-                      **options)
+    # the named arguments are defaults that an explicit tgs_options field overrides
+    base = dict(n_streams=streams, groups_per_item=groups, warps_per_block=warps, resident_netlist=levels,
+                mode=capi.MODE_PERSISTENT if mode == "persistent" else capi.MODE_GRAPH, value_pool=value_pool)
+    s = sim.Simulator(**{**base, **options})
     s.init(gpu, design, symbols, False, False)
     notes = {"schedule": schedule}
     if mode == "auto" and s.design_stats().get("resident_words"):
