@@ -84,6 +84,17 @@ def dist_init():
     return rank, ws
 
 
+def local_gpu(ws: int) -> int:
+    """This rank's GPU: LOCAL_RANK, wrapped onto the GPUs the node has (ranks
+    are independent replicas, so more ranks than GPUs share them)."""
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws == 1:
+        return lr
+    import torch
+
+    return lr % max(1, torch.cuda.device_count())
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -489,7 +500,7 @@ def run_gb300(a, rank, ws):
     from toucangpurt_gb300 import build, sim, workloads
 
     build.build()
-    gpu = int(os.environ.get("LOCAL_RANK", "0"))
+    gpu = local_gpu(ws)
     wd = Path(tempfile.mkdtemp(prefix="tgs_bench_"))
     dp, sp, info = make_design(a.workload, wd, rank, a.override)
     streams = a.streams or workloads.RUNS[a.workload]["streams"]

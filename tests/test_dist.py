@@ -60,3 +60,31 @@ def test_two_rank_replicas(tmp_path, built):
     assert [r[1] for r in res] == [160.0, 160.0]   # units summed over ranks
     assert [r[2] for r in res] == [2.0, 2.0]       # max over ranks
     assert res[0][3] != res[1][3]                  # ranks ran distinct stimulus
+
+
+@pytest.mark.gpu
+def test_bench_two_replicas(tmp_path):
+    """bench.py under torchrun with two ranks: each rank runs its own replica
+    of the 4K-LUT design (here both on the one GPU; ranks never wait on each
+    other's kernels, only on gloo barriers between steps), and rank 0 prints
+    one line whose value is the units of both ranks over the slower rank's
+    time."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    pytest.importorskip("torch")
+    root = Path(__file__).resolve().parents[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), str(root / "bench.py"), "--gpus", "2", "--workload", "small",
+           "--steps", "3", "--warmup", "3", "--no-cpu-baseline", "--no-baselines"]
+    r = subprocess.run(cmd, cwd=root, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["n_gpus"] == 2 and line["scaling"] == "weak" and line["value"] > 0
+    assert line["config"]["streams"] == 1
+    # two replicas' units over the slower rank's device time
+    assert abs(line["value"] - 2 * 2000 * 3 / (line["ms_per_step"] * 3 / 1000)) / line["value"] < 1e-6
