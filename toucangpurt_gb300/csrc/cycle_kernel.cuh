@@ -102,6 +102,15 @@ __device__ __forceinline__ void stsV4(uint32_t a, uint4 v) {
   asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
 }
 
+// Predicated (volatile) pair load: no access where c is false (0, 0 then).
+__device__ __forceinline__ uint2 ldsV2If(uint32_t a, bool c) {
+  uint2 v = make_uint2(0u, 0u);
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.shared.v2.u32 {%0, %1}, [%2];\n\t}"
+               : "+r"(v.x), "+r"(v.y)
+               : "r"(a), "r"(uint32_t(c)));
+  return v;
+}
+
 // Words of a level block / micro-partition record: staged in shared memory
 // (SH) or read from the schedule in global memory.
 template <bool SH>
@@ -116,6 +125,11 @@ struct Words {
   __device__ __forceinline__ uint2 pair(uint32_t i) const {
     if constexpr (SH) return ldsV2(s + 4u * i);
     else return __ldg(reinterpret_cast<const uint2 *>(g + i));
+  }
+  // words i, i + 1 where c holds, (0, 0) elsewhere (no access)
+  __device__ __forceinline__ uint2 pairIf(uint32_t i, bool c) const {
+    if constexpr (SH) return ldsV2If(s + 4u * i, c);
+    else return c ? __ldg(reinterpret_cast<const uint2 *>(g + i)) : make_uint2(0u, 0u);
   }
   __device__ __forceinline__ Words at(uint32_t off) const { return Words{g + off, s + 4u * off}; }
 };
@@ -619,13 +633,24 @@ __device__ __forceinline__ void runUnit(const KParams &p, const PartDesc &d, con
   __syncwarp();
 }
 
+// A warp's units [ub, ue) of one level of a one-group item, each unit's
+// record decoded while the previous one runs (defined with the one-group
+// helpers below).
+template <int SPW, bool SH>
+__device__ __forceinline__ void runUnitsOne(const KParams &p, const PartDesc &d, const Words<SH> blk,
+                                            const Words<SH> units, uint32_t ub, uint32_t ue, uint32_t vp, uint32_t tab,
+                                            uint32_t lane, uint32_t gb);
+
 template <int SPW, int G, bool SH>
 __device__ __forceinline__ void runLevel(const KParams &p, const PartDesc &d, const Words<SH> blk, uint32_t vp,
                                          uint32_t tab, uint32_t lane, uint32_t warp, uint32_t NW, uint32_t gb) {
   const uint32_t ub = blk[1 + warp], ue = blk[2 + warp];
   const Words<SH> units = blk.at(2 + NW);
   if (!(p.flags & kFlagProfileMP)) {
-    for (uint32_t u = ub; u < ue; ++u) runUnit<SPW, G, SH>(p, d, blk, units, u, vp, tab, lane, gb);
+    if constexpr (G == 1)
+      runUnitsOne<SPW, SH>(p, d, blk, units, ub, ue, vp, tab, lane, gb);
+    else
+      for (uint32_t u = ub; u < ue; ++u) runUnit<SPW, G, SH>(p, d, blk, units, u, vp, tab, lane, gb);
     return;
   }
   // the same with clock64 around every unit (cost-model samples)
@@ -745,6 +770,61 @@ __device__ __forceinline__ WarpLevelHead readWarpLevelHead(uint32_t blk, uint32_
   h.ue = ldsFixed(blk + 4u * (2u + warp));
   h.mp = blk;
   return h;
+}
+
+// The record of a unit (hdr: its header word) decoded as decodeWarpLevel1
+// does, for a level block staged or read from global memory.
+template <bool SH>
+__device__ __forceinline__ WarpLevel1 decodeUnit1(const Words<SH> mp, uint32_t hdr, uint32_t vp, uint32_t lane,
+                                                  bool constSlots) {
+  WarpLevel1 r;
+  r.sync = false;
+  r.ub = r.ue = 0u;
+  const uint32_t W = (hdr >> 2) & 63u, nMid = (hdr >> 8) & 255u, nWB = (hdr >> 16) & 63u;
+  r.simple = constSlots && (hdr & 3u) == kMPLut && (hdr & kMPCompact) != 0u && (hdr & kMPFastTop) == 0u &&
+             nMid == 0u;
+  r.act = r.simple && lane < W;
+  r.st = r.simple && lane < nWB;
+  const uint2 w = mp.at(kMPHeaderWords).pairIf(2u * lane, r.act);
+  r.lut = w.y >> 16;
+  r.aA = vp + 4u * (w.x & 0xFFFu);
+  r.aB = vp + 4u * ((w.x >> 12) & 0xFFFu);
+  r.aC = vp + 4u * ((w.x >> 24) | ((w.y & 15u) << 8));
+  r.wA = vp + 4u * ((w.y >> 4) & 0xFFFu);
+  return r;
+}
+
+template <int SPW, bool SH>
+__device__ __forceinline__ void runUnitsOne(const KParams &p, const PartDesc &d, const Words<SH> blk,
+                                            const Words<SH> units, uint32_t ub, uint32_t ue, uint32_t vp, uint32_t tab,
+                                            uint32_t lane, uint32_t gb) {
+  if (ub >= ue) return;
+  const bool cs = p.constSlots != 0;
+  WarpLevel1 now;
+  {
+    const Words<SH> mp = blk.at(units[ub] & kUnitOffsetMask);
+    now = decodeUnit1<SH>(mp, mp[0], vp, lane, cs);
+  }
+  for (uint32_t u = ub; u < ue; ++u) {
+    const bool more = u + 1 < ue;
+    const uint32_t A = ldsIf(now.aA, now.act, 0u), B = ldsIf(now.aB, now.act, 0u), C = ldsIf(now.aC, now.act, 0u);
+    // the next unit's record words go out beside this unit's operand loads
+    // (records do not change during the level; a unit that reads what the
+    // previous one wrote -- fused levels -- loads its operands after that
+    // unit's write-back and warp barrier, in the next iteration)
+    const uint32_t uw2 = more ? units[u + 1] : 0u;
+    // inactive lanes: A = B = C = 0 and lut = 0, an address inside the table
+    const uint32_t T = lookup<SPW>(tab, now.lut, A, B, C);
+    const Words<SH> mp2 = blk.at(uw2 & kUnitOffsetMask);
+    const uint32_t hdr2 = more ? mp2[0] : 0u;
+    if (now.simple) {
+      stsIf(now.wA, now.lut ? T : C, now.st);
+      __syncwarp();
+    } else {
+      runUnit<SPW, 1, SH>(p, d, blk, units, u, vp, tab, lane, gb);
+    }
+    if (more) now = decodeUnit1<SH>(mp2, hdr2, vp, lane, cs);
+  }
 }
 
 // Every exec level of one item of one stream group (G = 1), levels resident
