@@ -696,11 +696,6 @@ __device__ __forceinline__ uint32_t ldsFixed(uint32_t a) {
   asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
   return v;
 }
-__device__ __forceinline__ uint2 ldsFixed2(uint32_t a) {
-  uint2 v;
-  asm("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
-  return v;
-}
 
 // Predicated accesses: no access where c is false.  ldsIf keeps `v` there;
 // value-pool words are volatile as in ldsU32 / stsU32.
