@@ -125,3 +125,56 @@ def test_oracle_parser_agrees_on_sizes(design):
     assert od.mem_pool == info["mem_pool"]
     assert od.lut_ops == info["lut_ops"]
     assert od.lut_ops == sim.validate_file(dp, sp)
+
+
+_FUZZ_CHILD = r"""
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from toucangpurt_gb300 import capi, sim
+from pathlib import Path
+src, work, seed, n = Path(sys.argv[2]), Path(sys.argv[3]), int(sys.argv[4]), int(sys.argv[5])
+data = src.read_bytes()
+rng = np.random.default_rng(seed)
+accepted = rejected = 0
+for k in range(n):
+    b = bytearray(data)
+    mode = rng.integers(3)
+    if mode == 0:  # a few random bytes
+        for _ in range(rng.integers(1, 8)):
+            b[rng.integers(len(b))] = rng.integers(256)
+    elif mode == 1:  # a huge 64-bit count or offset
+        pos = int(rng.integers(len(b) - 8))
+        b[pos:pos + 8] = int(rng.integers(1 << 62)).to_bytes(8, "little")
+    else:  # a large 32-bit field
+        pos = int(rng.integers(len(b) - 4))
+        b[pos:pos + 4] = int(rng.integers(1 << 31)).to_bytes(4, "little")
+    p = work / "m.bin"
+    p.write_bytes(bytes(b))
+    try:
+        sim.validate_file(p)
+        accepted += 1
+        st = capi.RepackStats()
+        capi.check(capi.lib().tgs_repack_design(str(p).encode(), str(work / "r.bin").encode(), 0, 0, C.byref(st)))
+    except capi.TgsError:
+        rejected += 1
+print("fuzz", accepted, rejected)
+"""
+
+
+def test_mutated_design_files_never_crash(design, tmp_path):
+    """Random byte, 32-bit and 64-bit field mutations of a design file: the
+    bulk loader and the static checks reject it with an error code or accept
+    it (and then repacking it works); the process never crashes.  A child
+    process, so a crash is reported instead of ending the test run."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    dp, sp, _ = design
+    root = str(Path(__file__).resolve().parents[1])
+    r = subprocess.run([sys.executable, "-c", _FUZZ_CHILD, root, str(dp), str(tmp_path), "7", "300"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    accepted, rejected = map(int, r.stdout.split()[-2:])
+    assert accepted + rejected == 300 and rejected > 0
