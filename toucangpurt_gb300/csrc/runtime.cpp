@@ -506,7 +506,7 @@ void setupDevice(tgs_sim *h, int gpu) {
   TGS_CUDA(cudaSetDevice(gpu));
   TGS_CUDA(cudaGetDeviceProperties(&h->props, gpu));
   // sm_103a code only (the reference requires cc >= 7.0, ToucanSim.cu:34-43)
-  if (h->props.major != 10) throw Error(TGS_ERR_NO_DEVICE, std::string("this build targets sm_103a; found ") + h->props.name);
+  if (h->props.major != 10) throw Error(TGS_ERR_NO_DEVICE, std::string("the library is compiled for sm_103a; found ") + h->props.name);
   if (!h->props.cooperativeLaunch) throw Error(TGS_ERR_NO_DEVICE, "GPU does not support cooperative launch");
   h->device = gpu;
   if (!h->stream) TGS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
