@@ -467,6 +467,32 @@ typedef struct tgs_repack_stats {
 int tgs_repack_design(const char *in_path, const char *out_path, int lane_packing, int fast_luts,
                       tgs_repack_stats *stats);
 
+/* The exec-level schedule tgs_init would build for a design, computed on the
+ * host only (no GPU): the device image (renumbered value pool, lane packing
+ * unless lane_packing = 1, word-wide ops when fast_luts = 0 and more than one
+ * stream) and the gate-count schedule for `warps` warps per block and
+ * `groups` stream groups per item, with the schedule knobs mpart_lanes and
+ * levels_per_barrier (0 = defaults), for one block.  For checking and
+ * comparing schedules; tgs_get_design_stats reports the live one. */
+typedef struct tgs_schedule_stats {
+  uint64_t exec_levels;      /* exec levels of all partitions */
+  uint64_t blocks;           /* level blocks emitted (exec levels less the fused ones) */
+  uint64_t barriers;         /* level blocks that start with a block barrier */
+  uint64_t fused_levels;     /* exec levels merged into the block before them */
+  uint64_t schedule_words;   /* words of all level blocks */
+  uint32_t max_level_words;  /* largest level block */
+  uint32_t reserved0;
+  double makespan;           /* sum over level blocks of the most loaded warp's gate count */
+  double work;               /* sum of all units' gate counts */
+  double level_bound;        /* sum over level blocks of max(work / warps, largest unit): no schedule is shorter */
+  double list_bound;         /* sum over level blocks of work / warps + largest unit: a list schedule of
+                                single units (mpart_lanes 32, no fused levels) is not longer */
+  uint64_t reserved[3];
+} tgs_schedule_stats;
+int tgs_plan_schedule(const char *design_path, uint32_t warps, uint32_t groups, uint32_t mpart_lanes,
+                      uint32_t levels_per_barrier, int lane_packing, int fast_luts, uint32_t n_streams,
+                      tgs_schedule_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -156,6 +156,8 @@ for k in range(n):
         accepted += 1
         st = capi.RepackStats()
         capi.check(capi.lib().tgs_repack_design(str(p).encode(), str(work / "r.bin").encode(), 0, 0, C.byref(st)))
+        ss = capi.ScheduleStats()
+        capi.check(capi.lib().tgs_plan_schedule(str(p).encode(), 6, 4, 0, 2, 0, 0, 64, C.byref(ss)))
     except capi.TgsError:
         rejected += 1
 print("fuzz", accepted, rejected)
@@ -165,7 +167,8 @@ print("fuzz", accepted, rejected)
 def test_mutated_design_files_never_crash(design, tmp_path):
     """Random byte, 32-bit and 64-bit field mutations of a design file: the
     bulk loader and the static checks reject it with an error code or accept
-    it (and then repacking it works); the process never crashes.  A child
+    it (and then repacking it and planning its schedule work); the process
+    never crashes.  A child
     process, so a crash is reported instead of ending the test run."""
     import subprocess
     import sys

@@ -129,6 +129,15 @@ MLP_PARAMS = 5313
 
 # (name, argtypes) of every exported entry point; all return int status
 # except tgs_last_error / tgs_version.
+class ScheduleStats(C.Structure):
+    _fields_ = [
+        ("exec_levels", C.c_uint64), ("blocks", C.c_uint64), ("barriers", C.c_uint64), ("fused_levels", C.c_uint64),
+        ("schedule_words", C.c_uint64), ("max_level_words", C.c_uint32), ("reserved0", C.c_uint32),
+        ("makespan", C.c_double), ("work", C.c_double), ("level_bound", C.c_double), ("list_bound", C.c_double),
+        ("reserved", C.c_uint64 * 3),
+    ]
+
+
 class RepackStats(C.Structure):
     _fields_ = [("mparts_before", C.c_uint64), ("mparts_after", C.c_uint64), ("lut_ops", C.c_uint64),
                 ("fast_lut_ops", C.c_uint64), ("fast_mparts", C.c_uint64), ("exec_levels", C.c_uint64),
@@ -187,6 +196,8 @@ SIGNATURES = {
     "tgs_compact_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_pack_design": [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "tgs_repack_design": [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(RepackStats)],
+    "tgs_plan_schedule": [C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_uint32,
+                          C.POINTER(ScheduleStats)],
     "tgs_dump_state": [C.c_void_p, C.c_char_p],
     "tgs_read_signal_stream": [C.c_void_p, C.c_uint32, C.c_char_p, C.POINTER(C.c_uint64)],
     "tgs_enable_vcd": [C.c_void_p, C.c_char_p],

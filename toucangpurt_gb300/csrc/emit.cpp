@@ -776,6 +776,18 @@ void buildSchedule(const SimDesignInfo &d, DeviceImage &img, uint32_t NW, uint32
         }
       }
       total += mk;
+      {
+        double wsum = 0, umax = 0;
+        for (const auto &wu : plan)
+          for (const Unit &un : wu) {
+            wsum += un.c;
+            umax = std::max(umax, un.c);
+          }
+        out.planMakespan += mk;
+        out.planWork += wsum;
+        out.planLower += std::max(wsum / NW, umax);
+        out.planUpper += wsum / NW + umax;
+      }
       // does this block need a block barrier first?
       bool need = lv == 0;
       if (!need) {

@@ -62,6 +62,10 @@ struct Schedule {
   double makespan[2] = {0, 0};
   uint64_t barriers = 0, levels = 0;
   uint64_t fusedLevels = 0;  // exec levels merged into the block before them (levels per barrier > 1)
+  // per level block, summed: the most loaded warp's cost, all units' cost,
+  // max(cost / warps, largest unit) (no schedule does better) and
+  // cost / warps + largest unit (a list schedule of single units does no worse)
+  double planMakespan = 0, planWork = 0, planLower = 0, planUpper = 0;
 };
 
 // Schedule knobs (tgs_options.mpart_lanes / levels_per_barrier).

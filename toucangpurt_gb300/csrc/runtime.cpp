@@ -1976,6 +1976,44 @@ extern "C" int tgs_pack_design(const char *in, const char *out, uint32_t *mparts
   });
 }
 
+extern "C" int tgs_plan_schedule(const char *path, uint32_t warps, uint32_t groups, uint32_t mpartLanes,
+                                 uint32_t levelsPerBarrier, int lanePacking, int fastLuts, uint32_t nStreams,
+                                 tgs_schedule_stats *stats) {
+  return guard([&] {
+    if (!path || !stats) throw Error(TGS_ERR_ARG, "null argument");
+    if (warps < 1 || warps > 32) throw Error(TGS_ERR_ARG, "warps must be 1 to 32");
+    if (groups != 1 && groups != 2 && groups != 4 && groups != 8) throw Error(TGS_ERR_ARG, "groups must be 1, 2, 4 or 8");
+    SchedOpts so;
+    so.unitLanes = mpartLanes ? mpartLanes : 32u;
+    so.levelsPerBarrier = levelsPerBarrier ? levelsPerBarrier : 1u;
+    if (so.unitLanes != 32 && so.unitLanes != 64 && so.unitLanes != 128)
+      throw Error(TGS_ERR_ARG, "mpart_lanes must be 32, 64 or 128");
+    if (so.levelsPerBarrier != 1 && so.levelsPerBarrier != 2 && so.levelsPerBarrier != 4)
+      throw Error(TGS_ERR_ARG, "levels_per_barrier must be 1, 2 or 4");
+    auto bytes = readFileBytes(path);
+    SimDesignInfo d;
+    parseDesign(bytes.data(), bytes.size(), d);
+    validateDesign(d, nullptr);  // the static checks tgs_init runs before building the image
+    DeviceImage img;
+    buildImage(d, img, true, nullptr, lanePacking == 0, fastLuts == 0 && nStreams > 1);
+    Schedule s;
+    buildSchedule(d, img, warps, groups, nullptr, 1, 1, s, so);
+    tgs_schedule_stats st;
+    std::memset(&st, 0, sizeof st);
+    for (const auto &p : d.parts) st.exec_levels += p.exec_mParts.size();
+    st.blocks = s.levels;
+    st.barriers = s.barriers;
+    st.fused_levels = s.fusedLevels;
+    st.schedule_words = s.words.size();
+    st.max_level_words = s.maxLevelWords;
+    st.makespan = s.planMakespan;
+    st.work = s.planWork;
+    st.level_bound = s.planLower;
+    st.list_bound = s.planUpper;
+    *stats = st;
+  });
+}
+
 extern "C" int tgs_repack_design(const char *in, const char *out, int lanePacking, int fastLuts,
                                  tgs_repack_stats *stats) {
   return guard([&] {
