@@ -9,7 +9,9 @@
 // (src/SimEval.cu:69-148,1114-1343; restated here field by field), sets the
 // kernels' __device__ globals, and launches evalSingleCycle (one cycle per
 // cooperative launch, as ToucanSimulator::eval does, src/ToucanSim.cu:206-230)
-// or evalFreeRunningNCycles[_Large] (ToucanSim.cu:232-267).
+// or evalFreeRunningNCycles[_Large] (ToucanSim.cu:232-267).  The layout
+// (ref_layout.h) is checked on the CPU against the reference's own host code
+// (ref_layout_main.cpp, tests/test_ref_layout.py).
 //
 // Stimulus is applied between cycles on the host, as a reference testbench
 // does with setRegister (the hash is the oracle's, toucan_oracle.h).
@@ -30,6 +32,7 @@
 #include <vector>
 
 #include "ToucanGPUGenDataTypes.h"
+#include "ref_layout.h"
 
 using namespace toucanGPUSim;
 
@@ -45,40 +48,6 @@ namespace {
     }                                                                                 \
   } while (0)
 
-// Device structs of the reference (src/SimEval.cu:152-187), pointer fields as
-// 64-bit device addresses.
-struct RefPartPtrs {
-  uint64_t valuePool;
-  uint16_t valuePoolSize;
-  uint64_t constVecPool;
-  uint64_t netlist;
-  uint64_t lastLevelNetlistPtr;
-  uint32_t numOpsL0RegRead;
-  uint32_t numOpsL0ExgRead;
-  uint32_t numExecLevels;
-  uint64_t execMPartLevelInfo;
-  uint32_t numOpsLastExgWrite;
-  uint32_t numOpsLastRegWrite;
-  uint32_t numOpsLastMemWrite;
-  uint32_t numOpsLastPrint;
-  uint32_t numOpsLastStop;
-};
-static_assert(sizeof(RefPartPtrs) == 88 && offsetof(RefPartPtrs, netlist) == 24 &&
-                  offsetof(RefPartPtrs, execMPartLevelInfo) == 56 && offsetof(RefPartPtrs, numOpsLastStop) == 80,
-              "SimPartitionPtrs layout");
-struct RefLevelInfo {
-  uint32_t numMParts;
-  uint64_t mPartInfo;
-};
-static_assert(sizeof(RefLevelInfo) == 16, "SimMPartLevelInfo layout");
-struct RefMPartPtr {
-  uint32_t netlistOffset, netlistSize;
-};
-
-constexpr uint32_t kMagicLut = 0xfb709394u, kMagicVecRead = 0xfb809917u, kMagicMemRead = 0xccccccccu,
-                   kMagicVecOp = 0xbeef1234u;
-constexpr size_t kMaxLevels = 160, kLutSize = 4642;
-
 uint64_t mix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -89,51 +58,6 @@ uint64_t digest(const std::vector<uint8_t> &p) {
   uint64_t s = 0;
   for (size_t i = 0; i < p.size(); ++i) s += mix64((uint64_t(i) << 8) | p[i]);
   return s;
-}
-
-template <typename T>
-void appendRaw(std::vector<char> &b, const std::vector<T> &v) {
-  const char *d = reinterpret_cast<const char *>(v.data());
-  b.insert(b.end(), d, d + v.size() * sizeof(T));
-}
-void appendU32(std::vector<char> &b, uint32_t v) {
-  const char *d = reinterpret_cast<const char *>(&v);
-  b.insert(b.end(), d, d + 4);
-}
-// chunk padded to 16 bytes (appendToNetlistVec, SimEval.cu:1148-1154)
-void appendPadded(std::vector<char> &net, const char *d, size_t n) {
-  net.insert(net.end(), d, d + n);
-  for (size_t i = 0; i < (16 - n % 16) % 16; ++i) net.push_back(0);
-}
-
-// copyMicroPartToNetlist (SimEval.cu:69-148)
-std::vector<char> mpartBytes(const CGMicroPartInfo &m) {
-  std::vector<char> b;
-  if (m.isLUTPart) {
-    appendU32(b, kMagicLut);
-    appendU32(b, uint32_t(m.middleLevels.size()));
-    std::vector<char> sizes(kMaxLevels, 0);
-    sizes[0] = char(m.topLevel.size());
-    for (size_t i = 0; i < m.middleLevels.size(); ++i) sizes[1 + i] = char(m.middleLevels[i].size());
-    sizes[1 + m.middleLevels.size()] = char(m.lastLevel.size());
-    b.insert(b.end(), sizes.begin(), sizes.end());
-    appendRaw(b, m.topLevel);
-    for (auto &l : m.middleLevels) appendRaw(b, l);
-    appendRaw(b, m.lastLevel);
-  } else if (!m.vecRead.empty()) {
-    appendU32(b, kMagicVecRead);
-    appendU32(b, uint32_t(m.vecRead.size()));
-    appendRaw(b, m.vecRead);
-  } else if (!m.vecArithAndLogic.empty()) {
-    appendU32(b, kMagicVecOp);
-    appendU32(b, uint32_t(m.vecArithAndLogic.size()));
-    appendRaw(b, m.vecArithAndLogic);
-  } else {
-    appendU32(b, kMagicMemRead);
-    appendU32(b, uint32_t(m.memRead.size()));
-    appendRaw(b, m.memRead);
-  }
-  return b;
 }
 
 struct Module {
@@ -155,6 +79,15 @@ CUdeviceptr upload(const void *d, size_t n, std::vector<CUdeviceptr> &owned) {
   owned.push_back(p);
   return p;
 }
+
+// The layout on the GPU: device buffers and the cubin's __device__ globals.
+struct CudaSink : reflayout::Sink {
+  Module &M;
+  std::vector<CUdeviceptr> &owned;
+  CudaSink(Module &m, std::vector<CUdeviceptr> &o) : M(m), owned(o) {}
+  uint64_t upload(const void *d, size_t n) override { return ::upload(d, n, owned); }
+  void setGlobal(const char *name, const void *d, size_t n) override { CK(cuMemcpyHtoD(M.global(name, n), d, n)); }
+};
 
 struct Stim {
   uint64_t seed = 0;
@@ -233,78 +166,12 @@ int main(int argc, char **argv) {
     std::vector<CUdeviceptr> owned;
 
     // ---- copy_netlist_to_gpu -------------------------------------------
-    if (d.lut.size() != kLutSize) throw std::runtime_error("lut size");
-    CK(cuMemcpyHtoD(M.global("lutContent", kLutSize), d.lut.data(), kLutSize));
-    CUdeviceptr regDev = upload(d.regPool.data(), d.regPoolSize, owned);
-    CUdeviceptr memDev = upload(d.memPool.data(), d.memPoolSize, owned);
+    CudaSink sink(M, owned);
+    const reflayout::Layout L = reflayout::build(d, sink);
+    const CUdeviceptr regDev = L.reg, memDev = L.mem, exgDev = L.exg;
+    const size_t maxVp = L.maxVp;
+    const uint32_t n0 = L.n0, n1 = L.n1;
     std::vector<uint8_t> zeros(d.exchangePoolSize, 0);
-    CUdeviceptr exgDev = upload(zeros.data(), zeros.size(), owned);
-    CK(cuMemcpyHtoD(M.global("regPool", 8), &regDev, 8));
-    CK(cuMemcpyHtoD(M.global("memPool", 8), &memDev, 8));
-    CK(cuMemcpyHtoD(M.global("exchangePool", 8), &exgDev, 8));
-
-    std::vector<RefPartPtrs> parts;
-    size_t maxVp = 0;
-    for (const auto &p : d.parts) {
-      RefPartPtrs pp;
-      std::memset(&pp, 0, sizeof pp);
-      std::vector<char> net;
-      pp.valuePool = upload(p.valuePool.data(), p.valuePoolSize, owned);
-      pp.valuePoolSize = uint16_t(p.valuePoolSize);
-      maxVp = std::max<size_t>(maxVp, p.valuePoolSize);
-      pp.constVecPool = p.constVecPool.empty() ? 0 : upload(p.constVecPool.data(), p.constVecPool.size(), owned);
-      pp.numOpsL0RegRead = uint32_t(p.ops_l0_regRead.size());
-      if (pp.numOpsL0RegRead)
-        appendPadded(net, reinterpret_cast<const char *>(p.ops_l0_regRead.data()), p.ops_l0_regRead.size() * 8);
-      pp.numOpsL0ExgRead = uint32_t(p.ops_l0_exchangeRead.size());
-      if (pp.numOpsL0ExgRead)
-        appendPadded(net, reinterpret_cast<const char *>(p.ops_l0_exchangeRead.data()), p.ops_l0_exchangeRead.size() * 8);
-      std::vector<RefLevelInfo> levels;
-      for (const auto &lvl : p.exec_mParts) {
-        std::vector<RefMPartPtr> ptrs;
-        for (const auto &m : lvl) {
-          auto b = mpartBytes(m);
-          ptrs.push_back({uint32_t(net.size()), uint32_t(b.size())});
-          appendPadded(net, b.data(), b.size());
-        }
-        RefLevelInfo li;
-        std::memset(&li, 0, sizeof li);
-        li.numMParts = uint32_t(ptrs.size());
-        li.mPartInfo = ptrs.empty() ? 0 : upload(ptrs.data(), ptrs.size() * sizeof(RefMPartPtr), owned);
-        levels.push_back(li);
-      }
-      pp.numExecLevels = uint32_t(levels.size());
-      pp.execMPartLevelInfo = levels.empty() ? 0 : upload(levels.data(), levels.size() * sizeof(RefLevelInfo), owned);
-      pp.numOpsLastRegWrite = p.op_last_regWrite.count != 0;
-      pp.numOpsLastExgWrite = p.op_last_exchangeWrite.count != 0;
-      pp.numOpsLastMemWrite = uint32_t(p.ops_last_memWrite.size());
-      pp.numOpsLastPrint = uint32_t(p.ops_last_print.size());
-      pp.numOpsLastStop = uint32_t(p.ops_last_stop.size());
-      size_t lastOff = net.size();
-      if (pp.numOpsLastRegWrite) appendPadded(net, reinterpret_cast<const char *>(&p.op_last_regWrite), 8);
-      if (pp.numOpsLastExgWrite) appendPadded(net, reinterpret_cast<const char *>(&p.op_last_exchangeWrite), 8);
-      if (pp.numOpsLastMemWrite)
-        appendPadded(net, reinterpret_cast<const char *>(p.ops_last_memWrite.data()), p.ops_last_memWrite.size() * 24);
-      if (pp.numOpsLastPrint)
-        appendPadded(net, reinterpret_cast<const char *>(p.ops_last_print.data()), p.ops_last_print.size() * 4);
-      if (pp.numOpsLastStop)
-        appendPadded(net, reinterpret_cast<const char *>(p.ops_last_stop.data()), p.ops_last_stop.size() * 2);
-      pp.netlist = upload(net.data(), net.size(), owned);
-      pp.lastLevelNetlistPtr = pp.netlist + lastOff;
-      parts.push_back(pp);
-    }
-    CUdeviceptr partsDev = upload(parts.data(), parts.size() * sizeof(RefPartPtrs), owned);
-    CK(cuMemcpyHtoD(M.global("partitions", 8), &partsDev, 8));
-    if (d.regionPartitionIds.size() != 2) throw std::runtime_error("exactly two regions required");
-    uint32_t n0 = uint32_t(d.regionPartitionIds[0].size()), n1 = uint32_t(d.regionPartitionIds[1].size()),
-             nt = uint32_t(d.parts.size());
-    CK(cuMemcpyHtoD(M.global("numParts_Region0", 4), &n0, 4));
-    CK(cuMemcpyHtoD(M.global("numParts_Region1", 4), &n1, 4));
-    CK(cuMemcpyHtoD(M.global("numTotalParts", 4), &nt, 4));
-    std::vector<CUdeviceptr> msgPtrs;
-    for (auto &s : d.printMsgs) msgPtrs.push_back(upload(s.c_str(), s.size() + 1, owned));
-    CUdeviceptr msgsDev = upload(msgPtrs.data(), msgPtrs.size() * 8, owned);
-    CK(cuMemcpyHtoD(M.global("printMsgs", 8), &msgsDev, 8));
     uint8_t enablePrint = 0;
     CK(cuMemcpyHtoD(M.global("enablePrint", 1), &enablePrint, 1));
     CUdeviceptr stopDev = M.global("shouldStop", 4), realDev = M.global("realCycles", 4);
