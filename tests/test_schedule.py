@@ -29,10 +29,24 @@ def designs(tmp_path_factory, built):
 
 
 def plan(dp, warps=6, groups=4, lanes=0, lpb=0, packing=0, fast=0, streams=64):
+    return sim.plan_schedule(dp, warps, groups, lanes, lpb, packing, fast, streams)
+
+
+def test_c_abi_and_python_agree(designs):
     st = capi.ScheduleStats()
-    capi.check(capi.lib().tgs_plan_schedule(str(dp).encode(), warps, groups, lanes, lpb, packing, fast, streams,
-                                            C.byref(st)))
-    return {f: getattr(st, f) for f, _ in st._fields_ if not f.startswith("reserved")}
+    capi.check(capi.lib().tgs_plan_schedule(str(designs["mixed"]).encode(), 6, 4, 0, 2, 0, 0, 64, C.byref(st)))
+    assert {f: getattr(st, f) for f, _ in st._fields_ if not f.startswith("reserved")} == plan(designs["mixed"], lpb=2)
+
+
+def test_repack_then_plan(designs, tmp_path):
+    """A design rewritten the way tgs_init rewrites it plans like the original
+    (the image is built from it with the same transforms, which are
+    idempotent), with the same work."""
+    out = tmp_path / "r.bin"
+    st = sim.repack_design(designs["mixed"], out)
+    assert st["exec_levels"] > 0
+    a, b = plan(designs["mixed"]), plan(out)
+    assert a["exec_levels"] == b["exec_levels"] and abs(a["work"] - b["work"]) <= 1e-6 * a["work"]
 
 
 @pytest.mark.parametrize("name", list(DESIGNS))

@@ -327,6 +327,32 @@ def validate_file(design_path, symbol_path=None) -> int:
 _M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 
+def repack_design(design_path, out_path, lane_packing: int = 0, fast_luts: int = 0) -> dict:
+    """The design as tgs_init rewrites it, as a file (tgs_repack_design);
+    returns the micro-partition and LUT-op counts."""
+    st = capi.RepackStats()
+    check(lib().tgs_repack_design(str(design_path).encode(), str(out_path).encode(), lane_packing, fast_luts,
+                                  C.byref(st)))
+    return {f: getattr(st, f) for f, _ in capi.RepackStats._fields_ if f != "reserved"}
+
+
+def plan_schedule(design_path, warps: int = 6, groups: int = 4, mpart_lanes: int = 0, levels_per_barrier: int = 0,
+                  lane_packing: int = 0, fast_luts: int = 0, n_streams: int = 64) -> dict:
+    """The exec-level schedule tgs_init would build, computed on the host
+    (tgs_plan_schedule): level blocks, barriers, fused levels, and the plan's
+    makespan with its bounds (gate counts)."""
+    st = capi.ScheduleStats()
+    check(lib().tgs_plan_schedule(str(design_path).encode(), warps, groups, mpart_lanes, levels_per_barrier,
+                                  lane_packing, fast_luts, n_streams, C.byref(st)))
+    return {f: getattr(st, f) for f, _ in capi.ScheduleStats._fields_ if not f.startswith("reserved")}
+
+
+def device_reset(device: int = 0) -> None:
+    """Releases everything the library holds on the device (tgs_device_reset):
+    destroy every Simulator on it first."""
+    check(lib().tgs_device_reset(device))
+
+
 def mix64(z: np.ndarray) -> np.ndarray:
     """splitmix64 finaliser (Steele, Lea, Flood), vectorised over uint64."""
     with np.errstate(over="ignore"):
