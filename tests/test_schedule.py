@@ -106,3 +106,18 @@ def test_missing_design(tmp_path):
     with pytest.raises(capi.TgsError) as e:
         plan(tmp_path / "none.bin")
     assert e.value.code == capi.ERR_IO
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(DESIGNS))
+@pytest.mark.parametrize("streams,groups,lpb", [(64, 4, 0), (64, 4, 2), (8, 1, 0), (1, 1, 0)])
+def test_plan_matches_live_schedule(designs, name, streams, groups, lpb):
+    """The host-side plan is the schedule tgs_init builds: the same level
+    blocks, barriers and fused levels."""
+    dp = designs[name]
+    with sim.Simulator(n_streams=streams, groups_per_item=groups, warps_per_block=6, levels_per_barrier=lpb) as s:
+        s.init(0, dp, None, False, False)
+        st = s.design_stats()
+    p = plan(dp, 6, groups, 0, lpb, 0, 0, streams)
+    assert (st["exec_levels"], st["block_barriers"], st["fused_levels"]) == (p["blocks"], p["barriers"],
+                                                                              p["fused_levels"])
