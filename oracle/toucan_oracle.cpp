@@ -648,7 +648,7 @@ int orc_run(const orc_design *d, uint32_t n_streams, const uint32_t *cycles, con
 }
 
 orc_state *orc_state_new(const orc_design *d) {
-  auto *s = new orc_state{d, {}, {d, std::vector<uint8_t>(65536 + 64, 0), nullptr}};
+  auto *s = new orc_state{d, {}, {d, std::vector<uint8_t>(65536 + 64, 0), nullptr}, {}, {}};
   s->st.regs = d->regInit;
   s->st.mems = d->memInit;
   s->st.exg.assign(d->exgSize, 0);
